@@ -1,0 +1,461 @@
+"""Benchmark: ray-steps/s of the GB300 ray-integration path.
+
+Workload (default): 512^3 Gaussian-random-field density (|k|^-5/3 for
+2 pi/L <= |k| <= pi n/L, L = 5 mm, n_e = 5e24 (1 + 0.1 g), FP32), 1e7 rays at
+1064 nm (x, y ~ N(0, 1.5 mm), angles ~ N(0, 0.1 mrad)), phase on, then
+1024 x 1024 shadowgraphy, knife-edge schlieren (knife at x = 0) and
+interferometry (phase-weighted) detectors.  Synthetic, seeded inputs.
+
+One step = K1 FP32 volume build + K2b persistent FP32 trace of all rays +
+K3 three detectors, inputs resident in HBM (density 0.5 GB, volume 3.4 GB,
+rays 0.5 GB: all larger than the 129 MB L2, so no flush is needed).
+value = accepted ray-steps (one ray-step = one accepted Dormand-Prince step of
+one ray) per second over the timed steps.  e2e = the same through the public
+API (ElectronCube.solve + ray_transfer_matrix diagnostics) from pinned host
+rays to host results.  Beside it: the plain FP64 drop-in on a ray subset at
+the accuracy bar, the FP32 error against FP64, the roofline of the trace
+kernel, and the reference's CPU path timed on this host.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+Under torchrun each rank traces its own replica (weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "ray-steps/s at 512^3, 1e7 rays (FP32 persistent tracer, phase on, <=1 urad vs FP64)"
+UNIT = "ray-steps/s"
+ALG_BYTES_PHASE = 768  # 6 stages x 8 corners x 4 components x 4 B per ray-step (phase needs ne_nc)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--rays", type=float, default=1e7)
+    ap.add_argument("--L", type=float, default=5e-3)
+    ap.add_argument("--alpha", type=float, default=-5.0 / 3.0)
+    ap.add_argument("--delta", type=float, default=0.1)
+    ap.add_argument("--ne0", type=float, default=5e24)
+    ap.add_argument("--sigma", type=float, default=1.5e-3)
+    ap.add_argument("--div", type=float, default=0.1e-3)
+    ap.add_argument("--lwl", type=float, default=1064e-9)
+    ap.add_argument("--det", type=int, default=1024)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--fp64-rays", type=int, default=20000)
+    ap.add_argument("--check-rays", type=int, default=4000)
+    ap.add_argument("--cpu-rays", type=int, default=3000)
+    ap.add_argument("--ref-rays", type=int, default=1500)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--json-out", default="")
+    return ap.parse_args()
+
+
+def workload_config(a):
+    return {"workload": "grf%d_%grays_phase_3det%d" % (a.n, a.rays, a.det), "grid": [a.n] * 3, "L_m": a.L,
+            "spectrum_exponent": a.alpha, "delta": a.delta, "ne0_m3": a.ne0, "rays": int(a.rays),
+            "beam_sigma_m": a.sigma, "divergence_rad": a.div, "lwl_m": a.lwl,
+            "detectors": ["shadowgraphy", "schlieren_knife_x0", "interferometry"], "detector_bins": [a.det, a.det],
+            "detector_extent_mm": 12.0, "optics_f_mm": 100.0, "aperture_mm": 25.0,
+            "fp32_tol": {"rtol": 1e-6, "atol_cells": 1e-5, "atol_phase": 1e-5}, "seed": a.seed,
+            "l2": "inputs larger than L2 (density 0.5 GB, node volume 3.4 GB, rays 0.5 GB); no flush"}
+
+
+# ---------------------------------------------------------------------------- helpers
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read-only queries)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.TemporaryFile(mode="w+")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        for line in self.f:
+            p = [s.strip() for s in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------- our arm
+def run_ours(a):
+    import torch
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from turbulence_tracing_gb300 import core, turboGen
+    from turbulence_tracing_gb300 import particle_tracker as pt
+    from turbulence_tracing_gb300 import ray_transfer_matrix as rtm
+    from turbulence_tracing_gb300 import _lib
+
+    dev = torch.device("cuda", local)
+    n, L = a.n, a.L
+    Np = int(a.rays)
+    ne, x = turboGen.workload_field(n, L, a.alpha, a.delta, a.ne0, seed=a.seed + rank, dtype=torch.float32)
+    ext = float(x.max())
+    t_end = float(np.linspace(0.0, np.sqrt(8.0) * ext / 299792458.0, 2)[-1])
+    rng = np.random.default_rng(a.seed + 1000 * rank)
+    s0_host = np.empty((6, Np))
+    s0_host[0] = rng.normal(0.0, a.sigma, Np)
+    s0_host[1] = rng.normal(0.0, a.sigma, Np)
+    s0_host[2] = -ext
+    tx = np.tan(rng.normal(0.0, a.div, Np))
+    ty = np.tan(rng.normal(0.0, a.div, Np))
+    nrm = np.sqrt(1.0 + tx * tx + ty * ty)
+    s0_host[3] = 299792458.0 * tx / nrm
+    s0_host[4] = 299792458.0 * ty / nrm
+    s0_host[5] = 299792458.0 / nrm
+    del tx, ty, nrm
+    s0 = torch.as_tensor(s0_host, device=dev)
+
+    det = a.det
+    ext_mm = 6.0
+    f_mm, R_mm = 100.0, 25.0
+    relay = lambda mid: ([(_lib.OPTIC_M_TO_MM, 0, 0, 0), (_lib.OPTIC_DISTANCE, f_mm, 0, 0),
+                          (_lib.OPTIC_CIRC_APERTURE, R_mm, 0, 0), (_lib.OPTIC_LENS, f_mm, f_mm, 0),
+                          (_lib.OPTIC_DISTANCE, f_mm, 0, 0)] + mid +
+                         [(_lib.OPTIC_DISTANCE, f_mm, 0, 0), (_lib.OPTIC_CIRC_APERTURE, R_mm, 0, 0),
+                          (_lib.OPTIC_LENS, f_mm, f_mm, 0), (_lib.OPTIC_DISTANCE, f_mm, 0, 0)])
+    chain_shadow = relay([])
+    chain_knife = relay([(_lib.OPTIC_KNIFE_EDGE, 0.0, 0, 1.0)])
+    H = [torch.empty((det, det), dtype=torch.float64, device=dev) for _ in range(3)]
+    Hw = torch.empty((det, det), dtype=torch.float64, device=dev)
+    rng_mm = (-ext_mm, ext_mm)
+
+    # persistent buffers so the timed steps allocate nothing
+    vol = core.build_volume(ne, x, x, x, probing_axis=2, lwl=a.lwl)
+    out = core._ray_outputs(Np, dev, want_sf=True)
+    ws_bytes = _lib.lib().tt_trace_f32_workspace_bytes(__import__("ctypes").byref(vol.desc), Np)
+    wsp = core.workspace(ws_bytes, dev)
+    tr_ev = []
+
+    def step(record=False):
+        L_ = _lib.lib()
+        import ctypes
+
+        _lib.check(L_.tt_volume_build(ctypes.byref(vol.desc), ctypes.c_void_p(ne.data_ptr()), _lib.TT_F32,
+                                      core._stream()), "tt_volume_build")
+        e0 = e1 = None
+        if record:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+        core.trace_f32(vol, s0, t_end, ext, rtol=1e-6, atol=1e-5, atol_phase=1e-5, phase=True, ws=wsp, out=out)
+        if record:
+            e1.record()
+            tr_ev.append((e0, e1))
+        core.detect(out["rf"], chain_shadow, det, det, rng_mm, rng_mm, H=H[0])
+        core.detect(out["rf"], chain_knife, det, det, rng_mm, rng_mm, H=H[1])
+        core.detect(out["rf"], chain_shadow, det, det, rng_mm, rng_mm, weights=out["phase"], H=H[2], Hw=Hw)
+
+    launches_per_step = 1 + 4 + 3  # volume build; bin count/scan/scatter + trace; three detector kernels
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    ray_steps_step = int(out["nsteps"].sum().item())
+    st = out["status"]
+    n_bad = int((st != 0).sum().item())
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(a.steps):
+        step(record=True)
+    ev1.record()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    ms_total = ev0.elapsed_time(ev1)
+    trace_ms = [e0.elapsed_time(e1) for e0, e1 in tr_ev]
+    ms_step = ms_total / a.steps
+    if dist:
+        t = torch.tensor([ms_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = ray_steps_step * ws / (ms_step / 1e3)
+    rays_per_s = Np * ws / (ms_step / 1e3)
+
+    peak, peak_kind = peaks()
+    trace_ms_avg = float(np.mean(trace_ms))
+    alg_bytes = ray_steps_step * ALG_BYTES_PHASE
+    roof = {"kernel": "tt_trace_f32 (ray bucketing + persistent trace32_kernel)", "bound": "hbm",
+            "achieved": alg_bytes / (trace_ms_avg / 1e3) / 1e9, "peak": peak, "peak_kind": peak_kind,
+            "unit": "GB/s", "traffic": None,
+            "note": "algorithmic bytes = 768 B per ray-step (6 stages x 8 corners x 4 comps x 4 B); "
+                    "a face-clamped step reads one cell's 8 nodes once, so frac > 1 is cache reuse"}
+    roof["frac"] = roof["achieved"] / peak
+    res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic (seeded GRF density and Gaussian beam)",
+           "config": workload_config(a), "gpu_launches": launches_per_step * a.steps,
+           "roofline": roof, "clocks": clocks,
+           "detail": {"ray_steps_per_step": ray_steps_step, "rays_per_s": rays_per_s,
+                      "steps_per_ray": ray_steps_step / Np, "trace_ms": trace_ms_avg,
+                      "non_ok_rays": n_bad}}
+
+    if rank == 0 and not a.no_fp64:
+        res["fp64_dropin"], res["accuracy"] = fp64_compare(a, core, ne, x, s0_host, t_end, ext, out, rays_per_s / ws)
+    if not a.no_e2e:
+        res["e2e"] = e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist)
+    if rank == 0 and not a.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_baseline(a, ne, x)
+    if dist:
+        dist.destroy_process_group()
+    return res if rank == 0 else None
+
+
+def fp64_compare(a, core, ne, x, s0_host, t_end, ext, out32, rays_per_s32):
+    """Plain FP64 drop-in on a ray subset: (1) at the tolerance that meets the
+    accuracy bar, timed; (2) at rtol 1e-10 as the FP64 reference for the FP32 error."""
+    import torch
+
+    fields = core.calc_dndr(ne, x, x, x, lwl=a.lwl)
+    m = min(a.fp64_rays, s0_host.shape[1])
+    sub = torch.as_tensor(np.ascontiguousarray(s0_host[:, :m]), device="cuda")
+    core.trace_f64(fields, sub[:, :min(m, 256)], t_end, 2, ext, rtol=1e-8, atol=1e-11, phase=True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    o64 = core.trace_f64(fields, sub, t_end, 2, ext, rtol=1e-8, atol=1e-11, phase=True)
+    e1.record()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    steps64 = int(o64["nsteps"].sum().item())
+    c = min(a.check_rays, m)
+    ref = core.trace_f64(fields, sub[:, :c], t_end, 2, ext, rtol=1e-10, atol=1e-12, phase=True)
+    torch.cuda.synchronize()
+    rf_ref = ref["rf"].cpu().numpy()
+    ph_ref = ref["phase"].cpu().numpy()
+    acc = {}
+    for name, rf, ph in (("fp32", out32["rf"][:, :c].cpu().numpy(), out32["phase"][:c].cpu().numpy()),
+                         ("fp64_plain_rtol1e-8", o64["rf"][:, :c].cpu().numpy(), o64["phase"][:c].cpu().numpy())):
+        acc[name] = {"pos_over_L": float(np.abs(rf[0::2] - rf_ref[0::2]).max() / a.L),
+                     "angle_rad": float(np.abs(rf[1::2] - rf_ref[1::2]).max()),
+                     "phase_rad": float(np.abs(ph - ph_ref).max())}
+    acc["reference"] = "FP64 drop-in at rtol 1e-10, atol 1e-12 on %d rays (matches the CPU oracle to ~1e-10)" % c
+    acc["bars"] = {"pos_over_L": 1e-6, "angle_rad": 1e-6, "phase_rad": 1e-3}
+    del fields
+    torch.cuda.empty_cache()
+    f64 = {"rays": m, "rtol": 1e-8, "atol": 1e-11, "seconds": sec, "ray_steps": steps64,
+           "ray_steps_per_s": steps64 / sec, "rays_per_s": m / sec,
+           "fp32_speedup_equal_accuracy_rays_per_s": rays_per_s32 / (m / sec)}
+    return f64, acc
+
+
+def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
+    """Public API: ElectronCube.solve(precision='fp32', phase=True) from pinned host
+    rays, then three ray_transfer_matrix diagnostics on the returned rays."""
+    import torch
+
+    cube = pt.ElectronCube(x, x, x)
+    cube.external_ne(ne)
+    cube.calc_dndr(lwl=a.lwl)
+    cube.volume32()
+    pinned = torch.from_numpy(s0_host).pin_memory()
+    bins_scale = 1
+    import builtins
+
+    quiet = builtins.print
+
+    def one():
+        builtins.print = lambda *k, **kw: None
+        try:
+            cube.s0 = pinned
+            rf = cube.solve(precision="fp32", phase=True)
+        finally:
+            builtins.print = quiet
+        sh = rtm.Shadowgraphy(rf, focal_plane=0, L=100.0, R=25.0, Lx=2 * ext_mm, Ly=2 * ext_mm)
+        sh.solve()
+        sh.histogram(bin_scale=bins_scale, pix_x=det, pix_y=det)
+        ke = rtm.Schlieren_KE(rf, focal_plane=0, L=100.0, R=25.0, Lx=2 * ext_mm, Ly=2 * ext_mm)
+        ke.solve(offset=0.0, axis="x", direction=1)
+        ke.histogram(bin_scale=bins_scale, pix_x=det, pix_y=det)
+        it = rtm.Shadowgraphy(rf, focal_plane=0, L=100.0, R=25.0, Lx=2 * ext_mm, Ly=2 * ext_mm)
+        it.solve()
+        it.histogram(bin_scale=bins_scale, pix_x=det, pix_y=det, weights=cube.phase)
+        return int(cube.nsteps.sum()), sh.H.sum() + ke.H.sum() + it.Hw.sum()
+
+    one()
+    torch.cuda.synchronize()
+    k = max(1, min(a.steps, 3))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    tot = 0
+    for _ in range(k):
+        rs, _chk = one()
+        tot += rs
+    torch.cuda.synchronize()
+    sec = (time.perf_counter() - t0) / k
+    if dist:
+        t = torch.tensor([sec], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        sec = float(t.item())
+    Np = s0_host.shape[1]
+    h2d = Np * 6 * 8 + 3 * Np * 4 * 8 + Np * 8          # s0; rf re-uploaded by each diagnostic; phase weights
+    d2h = Np * (6 + 4 + 1) * 8 + Np * 2 * 4 + 3 * det * det * 8 + 3 * 4 * Np * 8
+    return {"value": (tot / k) * ws / sec, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "seconds_per_step": sec, "steps": k,
+            "path": "ElectronCube.solve(precision='fp32', phase=True) + Shadowgraphy, Schlieren_KE, "
+                    "phase-weighted Shadowgraphy histograms (numpy in, numpy out)"}
+
+
+def cpu_baseline(a, ne, x):
+    """The reference's CPU path (restated: oracle/ref_path.py) on a ray sample
+    through the same density, on this host's cores, in a subprocess that never
+    touches CUDA."""
+    with tempfile.TemporaryDirectory() as td:
+        dpath = os.path.join(td, "ne.npy")
+        np.save(dpath, ne.cpu().numpy())
+        jpath = os.path.join(td, "cpu.json")
+        cmd = [sys.executable, "-m", "oracle.ref_path", "--density", dpath, "--L", str(a.L), "--rays",
+               str(a.cpu_rays), "--sigma", str(a.sigma), "--div", str(a.div), "--lwl", str(a.lwl),
+               "--json", jpath]
+        r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=1200)
+        if r.returncode != 0:
+            return {"error": r.stderr[-500:]}
+        with open(jpath) as f:
+            d = json.load(f)
+    return {"value": d["ray_steps_per_s"], "unit": UNIT, "cores": d["procs"], "kind": "port",
+            "sample": "%d rays of the same workload (same density) traced by the reference's CPU path "
+                      "(global-step solve_ivp RK45 at rtol 1e-3/atol 1e-6 with RegularGridInterpolator "
+                      "lookups), in bundles over %d forked processes" % (d["rays"], d["procs"]),
+            "rays_per_s": d["rays_per_s"], "wall_s": d["wall"], "setup_s": d["setup_s"]}
+
+
+# ---------------------------------------------------------------------------- reference arm
+def run_reference(a):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return None
+    from oracle import ref_path as RP
+    from oracle import restated as R
+
+    ne, x = R.workload_density(a.n, a.L, a.alpha, a.delta, a.ne0, a.seed)
+    ne = ne.astype(np.float32)
+    cube = RP.RefCube(ne, x, x, x, lwl=a.lwl)
+    del ne
+    nproc = host_cores()
+    ext = float(x.max())
+    t_end = R.t_end(ext)
+    rng = np.random.default_rng(a.seed)
+    times, steps_done, rays_done = [], 0, 0
+    for i in range(a.warmup + a.steps):
+        s0 = R.gaussian_beam(a.ref_rays, a.sigma, a.div, ext, rng)
+        r = RP.run_pool(cube, s0, t_end, nproc)
+        if i >= a.warmup:
+            times.append(r["wall"])
+            steps_done += r["ray_steps"]
+            rays_done += a.ref_rays
+    sec = float(np.sum(times))
+    value = steps_done / sec
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * sec / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded GRF density and Gaussian beam)", "impl": "reference",
+            "config": workload_config(a),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nproc, "kind": "port",
+                             "sample": "%d rays per step through the full %d^3 field: the reference's CPU path "
+                                       "(global-step solve_ivp RK45, rtol 1e-3, RegularGridInterpolator) "
+                                       "restated, bundles over %d forked processes" % (a.ref_rays, a.n, nproc)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "detail": {"rays_per_s": rays_done / sec}}
+
+
+def main():
+    a = parse()
+    res = run_ours(a) if a.impl == "ours" else run_reference(a)
+    if res is not None:
+        line = json.dumps(res)
+        print(line)
+        if a.json_out:
+            with open(a.json_out, "w") as f:
+                f.write(line + "\n")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,219 @@
+/*
+ * turbotrace.h -- C ABI of libturbotrace.so, the GB300 (sm_103a) implementation
+ * of the ray-integration path of jdhare/turbulence_tracing.
+ *
+ * Conventions
+ *   - Every array pointer is DEVICE memory owned by the caller unless the
+ *     comment says "host".  The library keeps no pointer after a call returns.
+ *   - Volumes are C-ordered [ix][iy][iz] like the reference's numpy arrays.
+ *     Ray arrays are structure-of-arrays rows like the reference's (6, Np) s0
+ *     and (4, Np) rf: element (row, ray) lives at row * np + ray.
+ *   - stream is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *     All work is enqueued on it; no call synchronises the host unless noted.
+ *   - Scratch memory is a caller-provided device workspace whose size comes
+ *     from the matching *_workspace_bytes query.
+ *   - Every entry point returns a tt_status (0 = TT_OK).  Per-ray outcomes
+ *     are reported in int32 status arrays (tt_ray_status).
+ */
+#ifndef TURBOTRACE_H
+#define TURBOTRACE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TT_ABI_VERSION 1
+
+/* Per-ray cap on attempted integration steps when the caller passes 0. */
+#define TT_DEFAULT_MAX_STEPS (1LL << 22)
+
+typedef enum tt_status {
+    TT_OK = 0,
+    TT_ERR_INVALID_ARGUMENT = 1,
+    TT_ERR_WORKSPACE_TOO_SMALL = 2,
+    TT_ERR_CUDA = 3,
+    TT_ERR_CUFFT = 4,
+    TT_ERR_UNSUPPORTED = 5,
+    TT_ERR_TOO_LARGE = 6
+} tt_status;
+
+typedef enum tt_ray_status {
+    TT_RAY_OK = 0,              /* reached t_end */
+    TT_RAY_STEP_TOO_SMALL = 1,  /* solve_ivp's TOO_SMALL_STEP */
+    TT_RAY_MAX_STEPS = 2,       /* per-ray step cap hit (stiff); state left where it stopped */
+    TT_RAY_NAN = 3              /* non-finite state */
+} tt_ray_status;
+
+typedef enum tt_dtype { TT_F32 = 0, TT_F64 = 1 } tt_dtype;
+
+/* ABI version and error text.  tt_last_error_detail() is per host thread. */
+int tt_abi_version(void);
+const char* tt_strerror(int status);
+const char* tt_last_error_detail(void);
+
+/* ------------------------------------------------------------------------ */
+/* K1  calc_dndr -- replaces ElectronCube.calc_dndr,
+ *     particle_tracking/particle_tracker.py:220-237.
+ * omega = 2 pi c / lwl, n_c = 3.14207787e-4 omega^2, ne_nc = min(ne / n_c, ne_max),
+ * dndi = -0.5 c^2 numpy.gradient(ne_nc, coord_i, axis=i)  (edge_order 1,
+ * non-uniform coordinates allowed).  FP64 results are bit-identical to numpy.
+ * ne: (nx,ny,nz) of ne_dtype; x,y,z: device coordinate arrays (length nx,ny,nz). */
+size_t tt_calc_dndr_workspace_bytes(int nx, int ny, int nz);
+int tt_calc_dndr(const void* ne, int ne_dtype, int nx, int ny, int nz,
+                 const double* x, const double* y, const double* z,
+                 double lwl, double ne_max,
+                 double* ne_nc, double* dndx, double* dndy, double* dndz,
+                 double* omega_out /* host, may be NULL */,
+                 void* workspace, size_t workspace_bytes, void* stream);
+
+/* dndr -- replaces ElectronCube.dndr, particle_tracker.py:243-256 (the
+ * RegularGridInterpolator lookups built at :239-241): trilinear, fill 0
+ * outside the grid, NaN in -> NaN out.  pts: (3, npts) SoA; out: (nvol, npts)
+ * for the nvol volumes in vols[] (host array of device pointers, nvol <= 4). */
+int tt_dndr(const double* const* vols, int nvol, int nx, int ny, int nz,
+            const double* x, const double* y, const double* z,
+            const double* pts, int64_t npts, double* out, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* FP32 brick volume for the persistent tracer (K1, FP32 form).
+ * Nodes are float4 {H_a, H_b, H_c, ne_nc} with H = -0.5 d(ne_nc)/dx * spacing_c,
+ * i.e. the deflection per cell length of the probing axis.  Layout: the
+ * probing axis c is fastest; the transverse axes a, b are cut into 4x4-cell
+ * tiles stored with a one-node apron (5x5 node columns), each tile column cut
+ * into bricks of 8 nodes along c; tiles are ordered by Morton code inside 8x8
+ * super-tiles, super-tiles row-major.  Requires uniformly spaced coordinates. */
+typedef struct tt_volume {
+    int32_t n[3];          /* nodes along a, b, c */
+    int32_t axis[3];       /* physical axis (0=x, 1=y, 2=z) of a, b, c */
+    int32_t tiles[2];      /* 4-cell tiles along a, b */
+    int32_t supertiles[2]; /* 8x8-tile super-tiles along a, b */
+    int32_t bricks_c;      /* 8-node bricks along c */
+    int32_t reserved;
+    double origin[3];      /* coordinate (m) of node 0 along a, b, c */
+    double spacing[3];     /* node spacing (m) along a, b, c */
+    double omega;          /* laser angular frequency (rad/s) */
+    double ne_max;         /* clip applied to n_e/n_c */
+    int64_t n_float4;      /* float4 elements in the node buffer */
+    void* nodes;           /* device node buffer, 16-byte aligned, set by the caller */
+} tt_volume;
+
+/* Fill *vol (all fields but nodes) for a grid with host coordinate arrays and
+ * a probing axis (0=x, 1=y, 2=z); returns TT_ERR_UNSUPPORTED for non-uniform
+ * coordinates.  The node buffer needs vol->n_float4 * 16 bytes. */
+int tt_volume_plan(int nx, int ny, int nz, const double* x_host, const double* y_host,
+                   const double* z_host, int probing_axis, double lwl, double ne_max,
+                   tt_volume* vol);
+/* Write the node buffer from a density (nx,ny,nz) of ne_dtype. */
+int tt_volume_build(const tt_volume* vol, const void* ne, int ne_dtype, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* K2  trace -- replaces ElectronCube.solve + dsdt + dndr + ray_at_exit,
+ *     particle_tracker.py:312-380, 398-419.  Each ray integrates
+ *     x' = v, v' = grad from t = 0 to t_end with its own Dormand-Prince 5(4)
+ *     step control.  Outputs (any may be NULL): sf (6,np) state at t_end;
+ *     rf (4,np) [pos, angle, pos, angle] back-projected to the exit plane at
+ *     +extent along the probing axis (ray_at_exit); phase (np) = k0 int (n-1) ds
+ *     with n = sqrt(1 - ne_nc) (needs with_phase); status (np) tt_ray_status;
+ *     nsteps (np) accepted steps. */
+typedef struct tt_trace_opts {
+    double rtol;        /* FP64: as solve_ivp.  FP32: relative tolerance on velocity/phase */
+    double atol;        /* FP64: as solve_ivp (SI units).  FP32: absolute position tolerance in cells */
+    double atol_phase;  /* FP32 only: absolute phase tolerance (rad) */
+    int64_t max_steps;  /* per-ray cap on attempted steps; 0 = TT_DEFAULT_MAX_STEPS */
+    int32_t with_phase; /* integrate the phase as an extra state */
+    int32_t reserved;
+} tt_trace_opts;
+
+/* Plain FP64 drop-in: scipy RK45 controller per ray (safety 0.9, factors
+ * [0.2, 10], exponent -1/5, RMS norm over the ray's components, scipy's
+ * initial-step rule), lookups as tt_dndr.  probing_axis selects ray_at_exit's
+ * branch; extent is the exit-plane coordinate (cube.extent). */
+int tt_trace_f64(const double* dndx, const double* dndy, const double* dndz, const double* ne_nc,
+                 int nx, int ny, int nz, const double* x, const double* y, const double* z,
+                 double omega, const double* s0, int64_t np, double t_end,
+                 int probing_axis, double extent, const tt_trace_opts* opts,
+                 double* sf, double* rf, double* phase, int32_t* status, int32_t* nsteps,
+                 void* stream);
+
+/* Persistent FP32 tracer over a tt_volume: rays binned by entry tile in the
+ * volume's Morton order, one ray per thread pulled from a work queue, steps
+ * ended on cell faces so each step integrates one cell's trilinear
+ * polynomial, compensated (Neumaier) position/phase sums. */
+size_t tt_trace_f32_workspace_bytes(const tt_volume* vol, int64_t np);
+int tt_trace_f32(const tt_volume* vol, const double* s0, int64_t np, double t_end, double extent,
+                 const tt_trace_opts* opts, double* sf, double* rf, double* phase,
+                 int32_t* status, int32_t* nsteps, void* workspace, size_t workspace_bytes,
+                 void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* K3  detectors -- replaces Rays.__init__/solve/histogram and the filters of
+ *     particle_tracking/ray_transfer_matrix.py:37-195 (diagnostic chains at
+ *     :214-299).  Each ray of rf (4,n) is pushed through the optic chain
+ *     (host array; a diagnostic starts with TT_OPTIC_M_TO_MM as Rays.__init__
+ *     does), rejected rays become NaN, and the survivors are binned like
+ *     numpy.histogram2d over [x0,x1]x[y0,y1] (nbx x nby bins, last bin
+ *     closed) into H (nby, nbx) -- the transposed layout Rays.histogram leaves
+ *     in self.H.  Hw gets the same histogram weighted by weights (e.g. phase).
+ *     H/Hw are added to when accumulate != 0, else overwritten.  r_out (4,n),
+ *     if given, receives the rays after the chain (Rays.rf).  With H == NULL
+ *     only the chain runs (the module-level matrix and filter functions). */
+typedef enum tt_optic_kind {
+    TT_OPTIC_DISTANCE = 0,       /* p0 = d               distance(), :62-71 */
+    TT_OPTIC_LENS = 1,           /* p0 = f1, p1 = f2     lens(), :42-54 */
+    TT_OPTIC_CIRC_APERTURE = 2,  /* p0 = R   reject r^2 > R^2, :73-79 */
+    TT_OPTIC_CIRC_STOP = 3,      /* p0 = R   reject r^2 < R^2, :81-87 */
+    TT_OPTIC_ANNULUS_STOP = 4,   /* p0 = R1, p1 = R2  reject R1^2 < r^2 < R2^2 (one annulus of angular_filter, :89-111) */
+    TT_OPTIC_RECT_APERTURE = 5,  /* p0 = Lx, p1 = Ly  reject x^2 > Lx^2 AND y^2 > Ly^2, :128-136 */
+    TT_OPTIC_KNIFE_EDGE = 6,     /* p0 = offset, p1 = axis (0 = x, 2 = y), p2 = direction sign, :138-154 */
+    TT_OPTIC_M_TO_MM = 7         /* rows 0 and 2 times 1e3, m_to_mm() :37-40 */
+} tt_optic_kind;
+
+typedef struct tt_optic {
+    int32_t kind;
+    int32_t reserved;
+    double p[3];
+} tt_optic;
+
+#define TT_MAX_OPTICS 64
+
+int tt_detect(const double* rf, int64_t n, const tt_optic* chain_host, int n_optics,
+              int nbx, int nby, double x0, double x1, double y0, double y1,
+              const double* weights, double* H, double* Hw, double* r_out,
+              int accumulate, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* K4  Gaussian random fields -- replaces turboGen.gaussian3D_FFT,
+ *     gaussian_fields/turboGen.py:488-537.
+ * tt_grf_fft: M = 2N+1 points per axis; complex Gaussian noise Hermitian
+ * symmetrised (W(-k) = conj W(k), Re/Im variance 2 each as the reference's
+ * Wr + flip(Wr), Wi - flip(Wi)), times sqrt_p (the caller's k_func(|k|)
+ * square-rooted, on the half spectrum M x M x (N+1), |k| in cycles/sample),
+ * zero mean, inverse FFT / M^3, real part -> out (M,M,M) float64.
+ * Noise comes from Philox4x32-10 keyed by seed, or, when Wr and Wi (M^3,
+ * the reference's centred layout) are given, from those arrays. */
+size_t tt_grf_fft_workspace_bytes(int N);
+int tt_grf_fft(uint64_t seed, int N, const double* sqrt_p, const double* Wr, const double* Wi,
+               double* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* tt_grf_field: the band-limited field of the benchmark workloads on an n^3
+ * grid of side L: complex Gaussian noise (Philox4x32-10, counter = mode index)
+ * times |k|^(alpha/2) for kmin <= |k| <= kmax (rad/m), inverse real FFT,
+ * normalised to zero mean and unit variance g, then
+ * ne = ne0 (1 + delta g) clipped at >= 0, written as out_dtype. */
+size_t tt_grf_field_workspace_bytes(int n);
+int tt_grf_field(uint64_t seed, int n, double L, double alpha, double kmin, double kmax,
+                 double ne0, double delta, int out_dtype, void* out,
+                 void* workspace, size_t workspace_bytes, void* stream);
+
+/* Raw Philox4x32-10 blocks for counters (i, 0, 0, tag), i in [0, count), key = seed:
+ * out (4, count) uint32.  Exposed for known-answer tests of the generator. */
+int tt_philox(uint64_t seed, uint32_t tag, int64_t count, uint32_t* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TURBOTRACE_H */

@@ -1,0 +1,89 @@
+"""The C ABI without a GPU: the library loads, exports every entry point the
+header declares, and the host-only paths (argument checks, volume planning)
+behave."""
+import ctypes
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests.conftest import ROOT
+
+
+def _declared():
+    src = open(ROOT + "/include/turbotrace.h").read()
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(tt_\w+)\s*\(", src, re.M)))
+
+
+def test_header_symbols_exported():
+    from turbulence_tracing_gb300 import _lib
+
+    L = _lib.lib()
+    names = _declared()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(L, n), n
+        assert n in _lib.SIGNATURES, n
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.library_path()], capture_output=True, text=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if " T " in l}
+    assert set(names) <= exported
+
+
+def test_status_strings_and_version():
+    from turbulence_tracing_gb300 import _lib
+
+    L = _lib.lib()
+    assert L.tt_abi_version() == 1
+    for code in range(0, 7):
+        assert L.tt_strerror(code)
+
+
+def test_argument_checks_without_gpu():
+    from turbulence_tracing_gb300 import _lib
+
+    L = _lib.lib()
+    assert L.tt_calc_dndr(None, 1, 1, 4, 4, None, None, None, 1e-6, 1.0, None, None, None, None, None,
+                          None, 0, None) == 1
+    assert b"at least 2 points" in L.tt_last_error_detail()
+    opts = _lib.TTTraceOpts()
+    opts.rtol = 0.0
+    assert L.tt_trace_f64(None, None, None, None, 4, 4, 4, None, None, None, 1.0, None, 0, 1.0, 2, 1.0,
+                          ctypes.byref(opts), None, None, None, None, None, None) == 1
+    chain = (_lib.TTOptic * 1)()
+    chain[0].kind = 99
+    assert L.tt_detect(None, 0, chain, 1, 4, 4, -1.0, 1.0, -1.0, 1.0, None, ctypes.c_void_p(16), None, None, 0,
+                       None) == 1
+    chain[0].kind = _lib.OPTIC_KNIFE_EDGE
+    chain[0].p[2] = 0.0
+    assert L.tt_detect(None, 0, chain, 1, 4, 4, -1.0, 1.0, -1.0, 1.0, None, ctypes.c_void_p(16), None, None, 0,
+                       None) == 1
+    assert b"knife edge direction" in L.tt_last_error_detail()
+
+
+def test_volume_plan_geometry():
+    from turbulence_tracing_gb300 import _lib, core
+
+    x = np.linspace(-2.5e-3, 2.5e-3, 512)
+    v = core.volume_plan((512, 512, 512), x, x, x, 2, 1064e-9)
+    assert list(v.n) == [512, 512, 512] and list(v.axis) == [0, 1, 2]
+    assert list(v.tiles) == [128, 128] and list(v.supertiles) == [16, 16] and v.bricks_c == 64
+    assert v.n_float4 == 16 * 16 * 64 * 64 * 200
+    y = np.linspace(0, 1e-3, 30)
+    z = np.linspace(0, 2e-3, 70)
+    v = core.volume_plan((512, 30, 70), x, y, z, 0, 1064e-9)
+    assert list(v.axis) == [1, 2, 0] and list(v.n) == [30, 70, 512]
+    assert v.spacing[2] == pytest.approx(5e-3 / 511)
+    with pytest.raises(_lib.TTError):
+        core.volume_plan((10, 10, 10), np.cumsum(np.arange(1, 11.0)), x[:10], x[:10], 2, 1064e-9)
+
+
+def test_no_gpu_means_loud_failure():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from turbulence_tracing_gb300 import core
+
+    with pytest.raises(RuntimeError, match="CUDA"):
+        core.calc_dndr(np.zeros((4, 4, 4)), np.arange(4.0), np.arange(4.0), np.arange(4.0))

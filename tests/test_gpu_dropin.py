@@ -1,0 +1,134 @@
+"""The reference-facing API (particle_tracker / ray_transfer_matrix / turboGen
+drop-ins) driven the way the reference's notebook drives it."""
+import os
+import pickle
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import restated as R
+from tests.conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def test_null_notebook_flow(cuda, capsys):
+    """Notebook cells 1-4 (null test): no deflection."""
+    from turbulence_tracing_gb300 import particle_tracker as pt
+
+    x = np.linspace(-5e-3, 5e-3, 51)
+    null = pt.ElectronCube(x, x, x)
+    null.test_null()
+    null.calc_dndr()
+    np.random.seed(0)
+    null.init_beam(Np=20000, beam_size=2e-3, divergence=5e-3)
+    for precision in ("fp64", "fp32"):
+        rf = null.solve(precision=precision)
+        assert "Ray trace completed in" in capsys.readouterr().out
+        s0 = null.s0
+        T = 2 * x.max() / s0[5]
+        np.testing.assert_allclose(rf[0], s0[0] + s0[3] * T, rtol=0, atol=1e-11)
+        np.testing.assert_allclose(rf[1], np.arctan(s0[3] / s0[5]), rtol=0, atol=1e-12)
+        assert rf.shape == (4, 20000) and null.sf.shape == (6, 20000)
+
+
+def test_init_beam_matches_reference_draws(cuda):
+    from turbulence_tracing_gb300 import particle_tracker as pt
+
+    xs = np.linspace(-5e-3, 5e-3, 11)
+    for d in "xyz":
+        g = golden(f"beam_{d}")
+        cube = pt.ElectronCube(xs, xs * 0.8, xs * 1.2, probing_direction=d)
+        np.random.seed(7)
+        cube.init_beam(Np=50, beam_size=2e-3, divergence=5e-3)
+        assert np.array_equal(cube.s0, g["s0"]) and cube.extent == float(g["extent"])
+
+
+def test_reference_trace_and_attributes(cuda):
+    from turbulence_tracing_gb300 import particle_tracker as pt
+
+    d = golden("trace_grf16")
+    x = d["x"]
+    cube = pt.ElectronCube(x, x, x)
+    cube.external_ne(d["ne"])
+    cube.calc_dndr(lwl=1064e-9)
+    cube.s0 = d["s0"].copy()
+    rf = cube.solve(rtol=1e-10, atol=1e-12)
+    L = 2 * x.max()
+    assert np.abs(rf[0::2] - d["rf_tight"][0::2]).max() / L < 1e-8
+    assert np.abs(rf[1::2] - d["rf_tight"][1::2]).max() < 1e-8
+    # attributes the reference exposes
+    om, q, gx, gy, gz = __import__("oracle.tto", fromlist=["x"]).calc_dndr(d["ne"], x, x, x, 1064e-9, 1.0)
+    assert np.array_equal(cube.dndx, gx) and np.array_equal(cube.ne_nc, q) and cube.omega == om
+    pts = np.stack([x[3:9], x[2:8], x[1:7]])
+    assert np.array_equal(cube.dndr(pts)[0], cube.dndx_interp(pts.T))
+    # dsdt works as the ODE right-hand side, as in the reference
+    s = cube.s0.flatten()
+    ds = pt.dsdt(0.0, s, cube)
+    assert np.array_equal(ds.reshape(6, -1)[:3], cube.s0[3:])
+    assert np.array_equal(cube.ray_at_exit(), R.ray_at_exit(cube.sf, cube.extent))
+
+
+def test_save_and_pickle(cuda, tmp_path):
+    from turbulence_tracing_gb300 import particle_tracker as pt
+
+    x = np.linspace(-1e-3, 1e-3, 17)
+    cube = pt.ElectronCube(x, x, x)
+    cube.test_lens(n_e0=1e25, LR=0.5e-3)
+    cube.calc_dndr()
+    np.random.seed(2)
+    cube.init_beam(Np=100, beam_size=0.5e-3, divergence=1e-3)
+    rf = cube.solve()
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        cube.save_output_rays("rays")
+        assert np.array_equal(np.load("rays.npy"), rf)
+    finally:
+        os.chdir(cwd)
+    c2 = pickle.loads(pickle.dumps(cube))
+    rf2 = c2.solve()
+    assert np.array_equal(rf, rf2)
+
+
+def test_fp32_phase_through_api(cuda):
+    from turbulence_tracing_gb300 import particle_tracker as pt
+
+    ne, x = R.workload_density(48, 2e-3, -11 / 3, 0.2, 1e24, 5)
+    cube = pt.ElectronCube(x, x, x)
+    cube.external_ne(ne)
+    cube.calc_dndr(lwl=1064e-9)
+    cube.s0 = R.gaussian_beam(500, 0.5e-3, 0.05e-3, x.max(), np.random.default_rng(1))
+    rf32 = cube.solve(precision="fp32", phase=True)
+    ph32 = cube.phase.copy()
+    rf64 = cube.solve(precision="fp64", phase=True, rtol=1e-10, atol=1e-12)
+    assert np.abs(rf32[1::2] - rf64[1::2]).max() < 1e-6
+    assert np.abs(rf32[0::2] - rf64[0::2]).max() < 1e-6 * 2e-3
+    assert np.abs(ph32 - cube.phase).max() < 1e-3
+    assert (cube.status == 0).all()
+
+
+def test_shadowgraphy_on_traced_rays(cuda):
+    """Notebook cells 10-19: trace a lens, then the three diagnostics."""
+    from turbulence_tracing_gb300 import particle_tracker as pt
+    from turbulence_tracing_gb300 import ray_transfer_matrix as rtm
+
+    x = np.linspace(-5e-3, 5e-3, 101)
+    lens = pt.ElectronCube(x, x, x)
+    lens.test_lens(n_e0=5e25, LR=1e-3)
+    lens.calc_dndr()
+    np.random.seed(3)
+    lens.init_beam(Np=100000, beam_size=3e-3, divergence=10e-3)
+    lens.solve(precision="fp32")
+    sh = rtm.Shadowgraphy(r0=lens.rf, focal_plane=0, L=400, R=25, Lx=6, Ly=6)
+    df = rtm.Schlieren_DF(r0=lens.rf, focal_plane=0, L=400, R=25, Lx=6, Ly=6)
+    lf = rtm.Schlieren_LF(r0=lens.rf, focal_plane=0, L=400, R=25, Lx=6, Ly=6)
+    sh.solve()
+    df.solve(R=3)
+    lf.solve(R=3)
+    for o in (sh, df, lf):
+        o.histogram(bin_scale=25)
+    assert np.array_equal(df.H + lf.H, sh.H)
+    want = R.histogram(R.shadowgraphy(R.m_to_mm(lens.rf), 400, 25, 0), 6, 6, bin_scale=25)[0]
+    assert np.array_equal(sh.H, want)

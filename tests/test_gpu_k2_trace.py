@@ -1,0 +1,198 @@
+"""K2 (solve/dsdt/dndr/ray_at_exit, particle_tracker.py:243-380, 398-419) on
+the GPU vs the oracle.
+
+Bars (the benchmark spec): positions within 1e-6 of the box length, angles within
+1 urad, phase within 1e-3 rad of the FP64 oracle at rtol 1e-10."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import restated as R
+from tests.cases import LWL, errors, grf_case, oracle_trace
+from tests.conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+POS_BAR = 1e-6   # of box length
+ANG_BAR = 1e-6   # rad
+PHASE_BAR = 1e-3  # rad
+
+
+def _fields(ne, x, y=None, z=None, lwl=LWL):
+    from turbulence_tracing_gb300 import core
+
+    y = x if y is None else y
+    z = x if z is None else z
+    return core.calc_dndr(ne, x, y, z, lwl, 1.0)
+
+
+# ---------------------------------------------------------------- FP64 drop-in
+def test_f64_matches_oracle_same_tolerance(cuda):
+    """Same per-ray algorithm and rounding as the oracle: agreement far below the tolerance."""
+    from turbulence_tracing_gb300 import core
+
+    ne, x, s0 = grf_case(n=32, nrays=300)
+    f = _fields(ne, x)
+    for rtol, atol in [(1e-3, 1e-6), (1e-10, 1e-12)]:
+        out = core.trace_f64(f, s0, R.t_end(x.max()), 2, x.max(), rtol=rtol, atol=atol, phase=True)
+        ref = oracle_trace(ne, x, s0, rtol=rtol, atol=atol)
+        rf = out["rf"].cpu().numpy()
+        assert (out["status"].cpu().numpy() == 0).all()
+        close = np.all(np.abs(rf - ref["rf"]) <= 1e-11 * (1 + np.abs(ref["rf"])), axis=0)
+        assert close.mean() >= 0.99, close.mean()
+        assert np.abs(rf[1::2] - ref["rf"][1::2]).max() < 1e-4
+        assert np.array_equal(out["nsteps"].cpu().numpy()[close], ref["nacc"][close])
+        np.testing.assert_allclose(out["phase"].cpu().numpy()[close], ref["phase"][close], rtol=1e-9, atol=1e-12)
+
+
+def test_f64_vs_reference_golden(cuda):
+    from turbulence_tracing_gb300 import core
+
+    for name in ("trace_grf16", "trace_grf12_strong"):
+        d = golden(name)
+        x = d["x"]
+        f = _fields(d["ne"], x, lwl=float(d["lwl"]))
+        out = core.trace_f64(f, d["s0"], float(d["t_end"]), 2, x.max(), rtol=1e-10, atol=1e-12)
+        e = errors(out["rf"].cpu().numpy(), d["rf_tight"], 2 * x.max())
+        assert e["pos"] < 1e-8 and e["ang"] < 1e-8, e
+
+
+def test_f64_probing_directions(cuda):
+    from turbulence_tracing_gb300 import core
+
+    ne, x, _ = grf_case(n=24, L=1e-3, ne0=5e24, seed=3)
+    y = np.linspace(-0.6e-3, 0.6e-3, 20)
+    z = np.linspace(-0.4e-3, 0.4e-3, 18)
+    ne = ne[:, :20, :18]
+    f = _fields(ne, x, y, z)
+    for d, ax in (("x", 0), ("y", 1), ("z", 2)):
+        ext = {"x": x.max(), "y": y.max(), "z": z.max()}[d]
+        np.random.seed(4)
+        s0 = R.init_beam(100, 0.3e-3, 2e-3, ext, d)
+        out = core.trace_f64(f, s0, R.t_end(ext), ax, ext, rtol=1e-10, atol=1e-12)
+        ref = oracle_trace(ne, x, s0, y=y, z=z, direction=d, phase=False)
+        e = errors(out["rf"].cpu().numpy(), ref["rf"], 2 * ext)
+        assert e["pos"] < 1e-9 and e["ang"] < 1e-9, (d, e)
+
+
+def test_f64_edge_cases(cuda):
+    from turbulence_tracing_gb300 import core
+
+    ne, x, s0 = grf_case(n=16, nrays=6)
+    f = _fields(ne, x)
+    s0 = s0.copy()
+    s0[0, 1] = np.nan                 # NaN ray
+    s0[0, 2] = 5 * x.max()            # misses the box
+    out = core.trace_f64(f, s0, R.t_end(x.max()), 2, x.max())
+    st = out["status"].cpu().numpy()
+    assert st[1] == 3 and st[0] == 0 and st[2] == 0
+    rf = out["rf"].cpu().numpy()
+    assert rf[0, 2] == pytest.approx(s0[0, 2] + s0[3, 2] / s0[5, 2] * 2 * x.max(), rel=1e-12)
+    empty = core.trace_f64(f, np.zeros((6, 0)), R.t_end(x.max()), 2, x.max())
+    assert empty["rf"].shape == (4, 0)
+
+
+# ---------------------------------------------------------------- FP32 persistent tracer
+def _f32(ne, x, s0, phase=True, rtol=1e-6, atol=1e-5, y=None, z=None, axis=2, ext=None):
+    from turbulence_tracing_gb300 import core
+
+    y = x if y is None else y
+    z = x if z is None else z
+    ext = x.max() if ext is None else ext
+    vol = core.build_volume(ne, x, y, z, probing_axis=axis, lwl=LWL)
+    return core.trace_f32(vol, s0, R.t_end(ext), ext, rtol=rtol, atol=atol, phase=phase)
+
+
+def test_f32_meets_accuracy_bars_config1_shape(cuda):
+    """128^3 GRF, L = 2 mm, k^-11/3, delta 0.2, 1e24 m^-3, 1064 nm, Gaussian beam
+    sigma 0.5 mm, divergence 0.05 mrad (the CPU-runnable workload) on 1500 rays."""
+    ne, x, s0 = grf_case(n=128, L=2e-3, nrays=1500, sigma_frac=0.25)
+    out = _f32(ne, x, s0)
+    ref = oracle_trace(ne, x, s0)
+    st = out["status"].cpu().numpy()
+    assert (st == 0).all()
+    e = errors(out["rf"].cpu().numpy(), ref["rf"], 2 * x.max(), out["phase"].cpu().numpy(), ref["phase"])
+    assert e["pos"] <= POS_BAR and e["ang"] <= ANG_BAR and e["phase"] <= PHASE_BAR, e
+    # about one step per cell crossed, far fewer than the oracle's
+    n = out["nsteps"].cpu().numpy()
+    assert n.max() < 3 * 128 and n.mean() > 100
+
+
+def test_f32_strong_field_and_directions(cuda):
+    """Stronger, steeper field (delta 0.3, 5e25 m^-3) and the three probing axes."""
+    ne, x, _ = grf_case(n=40, L=1e-3, alpha=-5 / 3, delta=0.3, ne0=5e25, seed=7)
+    y = np.linspace(-0.5e-3, 0.5e-3, 36)
+    z = np.linspace(-0.5e-3, 0.5e-3, 33)
+    ne = ne[:, :36, :33]
+    for d, ax in (("z", 2), ("x", 0), ("y", 1)):
+        ext = {"x": x.max(), "y": y.max(), "z": z.max()}[d]
+        np.random.seed(8)
+        s0 = R.init_beam(400, 0.35e-3, 1e-3, ext, d)
+        out = _f32(ne, x, s0, y=y, z=z, axis=ax, ext=ext, rtol=1e-7)
+        ref = oracle_trace(ne, x, s0, y=y, z=z, direction=d)
+        assert (out["status"].cpu().numpy() == 0).all()
+        e = errors(out["rf"].cpu().numpy(), ref["rf"], 2 * ext, out["phase"].cpu().numpy(), ref["phase"])
+        assert e["pos"] <= POS_BAR and e["ang"] <= ANG_BAR and e["phase"] <= PHASE_BAR, (d, e)
+
+
+def test_f32_slab_closed_form(cuda):
+    from tests.test_oracle_golden import slab_closed_form
+
+    x = np.linspace(-5e-3, 5e-3, 41)
+    ne = 1e25 * (1.0 + 8 * np.meshgrid(x, x, x, indexing="ij")[0] / x.max())
+    np.random.seed(11)
+    s0 = R.init_beam(200, 2e-3, 10e-3, x.max(), "z")
+    from turbulence_tracing_gb300 import core
+
+    vol = core.build_volume(ne, x, x, x, 2, lwl=1053e-9)
+    out = core.trace_f32(vol, s0, R.t_end(x.max()), x.max(), rtol=1e-7)
+    want = slab_closed_form(s0, x.max())
+    rf = out["rf"].cpu().numpy()
+    e = errors(rf, want, 2 * x.max())
+    assert e["pos"] <= POS_BAR and e["ang"] <= ANG_BAR, e
+
+
+def test_f32_edge_rays(cuda):
+    """Rays outside the box, leaving through a side, starting before the box, NaN; empty call."""
+    from turbulence_tracing_gb300 import core
+
+    ne, x, _ = grf_case(n=24, L=1e-3, seed=9)
+    ext = x.max()
+    c = R.C_LIGHT
+    s0 = np.zeros((6, 6))
+    s0[:, 0] = [0.0, 0.0, -ext, 0.0, 0.0, c]                   # on axis
+    s0[:, 1] = [3 * ext, 0.0, -ext, 0.0, 0.0, c]               # misses the box
+    s0[:, 2] = [0.9 * ext, 0.0, -ext, 0.2 * c, 0.0, 0.98 * c]  # leaves through +x
+    s0[:, 3] = [0.1 * ext, -0.2 * ext, -2 * ext, 0.0, 0.0, c]  # starts before the box
+    s0[:, 4] = [np.nan, 0.0, -ext, 0.0, 0.0, c]                # NaN
+    s0[:, 5] = [ext, ext, -ext, 0.0, 0.0, c]                   # on the box corner line
+    s0[3:, 2] *= c / np.linalg.norm(s0[3:, 2])
+    vol = core.build_volume(ne, x, x, x, 2, lwl=LWL)
+    out = core.trace_f32(vol, s0, R.t_end(ext), ext, rtol=1e-7, phase=True)
+    ref = oracle_trace(ne, x, s0)
+    st = out["status"].cpu().numpy()
+    assert st[4] == 3 and np.all(np.delete(st, 4) == 0)
+    rf = out["rf"].cpu().numpy()
+    keep = [0, 1, 2, 3, 5]
+    e = errors(rf[:, keep], ref["rf"][:, keep], 2 * ext, out["phase"].cpu().numpy()[keep], ref["phase"][keep])
+    assert e["pos"] <= POS_BAR and e["ang"] <= ANG_BAR and e["phase"] <= PHASE_BAR, e
+    empty = core.trace_f32(vol, np.zeros((6, 0)), R.t_end(ext), ext)
+    assert empty["rf"].shape == (4, 0)
+
+
+def test_f32_null_field_is_straight(cuda):
+    """test_null: output rays are the straight-line projection of the input rays."""
+    from turbulence_tracing_gb300 import core
+
+    x = np.linspace(-5e-3, 5e-3, 65)
+    ne = np.zeros((65, 65, 65))
+    np.random.seed(1)
+    s0 = R.init_beam(5000, 2e-3, 5e-3, x.max(), "z")
+    vol = core.build_volume(ne, x, x, x, 2, lwl=1053e-9)
+    out = core.trace_f32(vol, s0, R.t_end(x.max()), x.max(), phase=True)
+    rf = out["rf"].cpu().numpy()
+    T = 2 * x.max() / s0[5]
+    want = np.stack([s0[0] + s0[3] * T, np.arctan(s0[3] / s0[5]), s0[1] + s0[4] * T, np.arctan(s0[4] / s0[5])])
+    e = errors(rf, want, 2 * x.max())
+    assert e["pos"] < 1e-9 and e["ang"] < 1e-9, e
+    assert np.abs(out["phase"].cpu().numpy()).max() == 0.0

@@ -1,0 +1,185 @@
+"""Pin the CPU oracle against fixtures produced by the reference itself
+(tests/golden/make_golden.py imports particle_tracker, ray_transfer_matrix,
+turboGen and calculate_spectrum_3d).  No GPU."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import restated as R
+from oracle import tto
+from tests.conftest import GOLDEN, golden
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "dndr_*.npz"))),
+                         ids=lambda p: os.path.basename(p))
+def test_calc_dndr_and_lookup_bit_exact(path):
+    d = np.load(path)
+    om, q, gx, gy, gz = tto.calc_dndr(d["ne"], d["x"], d["y"], d["z"], float(d["lwl"]), float(d["ne_max"]))
+    assert om == float(d["omega"])
+    for a, k in [(q, "ne_nc"), (gx, "dndx"), (gy, "dndy"), (gz, "dndz")]:
+        assert np.array_equal(a, d[k]), k
+    g = np.stack([tto.interp(v, d["x"], d["y"], d["z"], d["pts"]) for v in (gx, gy, gz)])
+    assert np.array_equal(g, d["grad"])
+
+
+def test_trace_matches_reference_tight():
+    """Per-ray RK45 at rtol 1e-10 vs the reference's global-step solve_ivp at rtol 1e-10."""
+    for name in ("trace_grf16", "trace_grf12_strong"):
+        d = golden(name)
+        x = d["x"]
+        om, q, gx, gy, gz = tto.calc_dndr(d["ne"], x, x, x, float(d["lwl"]), 1.0)
+        r = tto.trace(gx, gy, gz, x, x, x, d["s0"], float(d["t_end"]), 1e-10, 1e-12)
+        assert (r["status"] == 0).all()
+        rf = R.ray_at_exit(r["sf"], x.max())
+        L = 2 * x.max()
+        assert np.abs(rf[0::2] - d["rf_tight"][0::2]).max() / L < 1e-8
+        assert np.abs(rf[1::2] - d["rf_tight"][1::2]).max() < 1e-8
+        # the reference default (rtol 1e-3) is far looser: documents why the oracle runs tight
+        assert np.abs(d["rf_default"][1::2] - d["rf_tight"][1::2]).max() > 1e-6
+
+
+def slab_closed_form(s0, ext, n0=1e25, s=8, lwl=1053e-9):
+    """test_slab (particle_tracker.py:158-167) has a constant gradient, so a ray
+    that stays in the box crosses it on a parabola: vx grows linearly in time."""
+    _, nc = R.critical_density(lwl)
+    a = -0.5 * R.C_LIGHT ** 2 * n0 * s / ext / nc
+    t_cross = 2 * ext / s0[5]
+    vx = s0[3] + a * t_cross
+    x_exit = s0[0] + s0[3] * t_cross + 0.5 * a * t_cross ** 2
+    y_exit = s0[1] + s0[4] * t_cross
+    return np.stack([x_exit, np.arctan(vx / s0[5]), y_exit, np.arctan(s0[4] / s0[5])])
+
+
+def test_slab_parabola():
+    """Tight oracle reproduces the closed form; the reference's default solve()
+    does not (its global steps straddle the box exit where the field drops to
+    0), which is why parity is asserted against the tight oracle."""
+    d = golden("slab_default")
+    x = d["x"]
+    s0 = d["s0"]
+    ext = x.max()
+    want = slab_closed_form(s0, ext)
+    ne = 1e25 * (1.0 + 8 * np.meshgrid(x, x, x, indexing="ij")[0] / ext)
+    om, q, gx, gy, gz = tto.calc_dndr(ne, x, x, x, 1053e-9, 1.0)
+    r = tto.trace(gx, gy, gz, x, x, x, s0, R.t_end(ext), 1e-10, 1e-12)
+    rf = R.ray_at_exit(r["sf"], ext)
+    np.testing.assert_allclose(rf[1::2], want[1::2], rtol=0, atol=1e-8)
+    np.testing.assert_allclose(rf[0::2], want[0::2], rtol=0, atol=1e-10)
+    assert np.abs(d["rf"][1] - want[1]).max() > 1e-3  # reference default is ~10% off
+
+
+def test_init_beam_same_draws():
+    for dname in "xyz":
+        d = golden(f"beam_{dname}")
+        np.random.seed(7)
+        s0 = R.init_beam(50, 2e-3, 5e-3, float(d["extent"]), dname)
+        assert np.array_equal(s0, d["s0"])
+
+
+def test_ray_at_exit():
+    for dname in "xyz":
+        d = golden(f"exit_{dname}")
+        assert np.array_equal(R.ray_at_exit(d["sf"], float(d["extent"]), dname), d["rf"])
+
+
+def test_test_densities():
+    xs = np.linspace(-5e-3, 5e-3, 11)
+    x, y, z = xs, xs * 0.8, xs * 1.2
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    want = {
+        "test_null": np.zeros_like(X),
+        "test_slab": 1e25 * (1.0 + 8 * X / x.max()),
+        "test_linear_cos": 2e23 * (1.0 + 0.1 * X / x.max()) * (1 + 0.1 * np.cos(2 * np.pi * Y / 1)),
+        "test_exponential_cos": 1e24 * 10 ** (X / 2e-3) * (1 + np.cos(2 * np.pi * Y / 1e-3)),
+        "test_lens": 5e25 * np.exp(-np.sqrt(X ** 2 + Y ** 2) ** 2 / 1e-3 ** 2),
+        "test_liner": 2e27 * np.exp(-np.sqrt(X ** 2 + Z ** 2) ** 2 / 1e-3 ** 2),
+    }
+    for k, v in want.items():
+        assert np.array_equal(golden(f"dens_{k}")["ne"], v), k
+
+
+def test_rtm_chains_and_histograms():
+    d = golden("rtm")
+    r0 = d["r0"]
+    mm = R.m_to_mm(r0)
+    chains = {
+        "Shadowgraphy": lambda r: R.shadowgraphy(r, 400, 25, 0),
+        "Schlieren_DF": lambda r: R.schlieren_df(r, 400, 25, 3, 0),
+        "Schlieren_LF": lambda r: R.schlieren_lf(r, 400, 25, 3, 0),
+        "AFR": lambda r: R.afr(r, 100, 25, np.arange(0, 6, 0.5), 5),
+    }
+    dims = {"Shadowgraphy": (6, 6), "Schlieren_DF": (6, 6), "Schlieren_LF": (6, 6), "AFR": (15, 10)}
+    for k, f in chains.items():
+        rf = f(mm.copy())
+        np.testing.assert_array_equal(np.isnan(rf), np.isnan(d[f"{k}_rf"]))
+        np.testing.assert_allclose(rf, d[f"{k}_rf"], rtol=1e-13, atol=1e-12)
+        Lx, Ly = dims[k]
+        H, xe, ye = R.histogram(rf, Lx, Ly, bin_scale=25)
+        assert np.array_equal(H, d[f"{k}_H"])
+        assert np.array_equal(xe, d[f"{k}_xe"]) and np.array_equal(ye, d[f"{k}_ye"])
+        H2, _, _ = R.histogram(rf, Lx, Ly, bin_scale=10, pix_x=500, pix_y=300)
+        assert np.array_equal(H2, d[f"{k}_H2"])
+        # C restatement of the binning rule gives the same counts
+        Hc, _, _ = tto.histogram2d(rf[0], rf[2], 3448 // 25, 2574 // 25, (-Lx / 2, Lx / 2), (-Ly / 2, Ly / 2))
+        assert np.array_equal(Hc, d[f"{k}_H"])
+    rr = r0 * 1e3
+    assert np.array_equal(R.knife_edge(rr.copy(), 0.5, "x", 1), d["knife_x_pos"], equal_nan=True)
+    assert np.array_equal(R.knife_edge(rr.copy(), -0.5, "y", -1), d["knife_y_neg"], equal_nan=True)
+    assert np.array_equal(R.rect_aperture(rr.copy(), 2.0, 3.0), d["rect"], equal_nan=True)
+    np.testing.assert_allclose(R.lens(rr.copy(), 100.0, 50.0), d["lens"], rtol=1e-15, atol=0)
+    np.testing.assert_allclose(R.distance(rr.copy(), 123.0), d["dist"], rtol=1e-13, atol=1e-13)
+
+
+def test_dark_plus_light_field_is_shadowgraphy():
+    """Notebook cell 19: LF + DF = shadowgraphy (stop uses <, aperture uses >)."""
+    d = golden("rtm")
+    assert np.array_equal(d["Schlieren_DF_H"] + d["Schlieren_LF_H"], d["Shadowgraphy_H"])
+
+
+def test_histogram_edge_rule():
+    xe = np.linspace(-3, 3, 7)
+    xs = np.concatenate([xe, [np.nan, -3.0000001, 3.0000001]])
+    ys = np.zeros_like(xs)
+    Hn, _, _ = np.histogram2d(xs[~np.isnan(xs)], ys[~np.isnan(xs)], bins=[6, 1], range=[[-3, 3], [-1, 1]])
+    Hc, _, _ = tto.histogram2d(xs, ys, 6, 1, (-3, 3), (-1, 1))
+    assert np.array_equal(Hc, Hn.T)
+    assert Hc[0, -1] == 2  # right edge closed
+
+
+def test_gaussian3D_FFT_restatement():
+    d = golden("grf_fft")
+
+    def k41(k):
+        return k ** (-5 / 3)
+
+    sig = R.gaussian3D_FFT(int(d["N"]), k41, Wr=d["Wr"], Wi=d["Wi"])
+    np.testing.assert_allclose(sig, d["signal"], rtol=0, atol=1e-14 * np.abs(d["signal"]).max())
+
+
+def test_spectrum_restatement():
+    d = golden("spectrum")
+    kb, sp = R.spectrum_3D_scalar(d["data"], float(d["dx"]), k_bin_num=20)
+    np.testing.assert_allclose(kb, d["kb"], rtol=1e-14)
+    np.testing.assert_allclose(sp, d["sp"], rtol=1e-10, equal_nan=True)
+
+
+def test_philox_known_answers():
+    """Random123 known-answer vectors for philox4x32-10."""
+    kat = [((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+           ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+           ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+            (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1))]
+    for c, k, want in kat:
+        got = R.philox4x32_10(*c, *k)
+        assert tuple(int(v) for v in got) == want
+
+
+def test_workload_field_statistics():
+    ne, x = R.workload_density(32, 2e-3, -11 / 3, 0.2, 1e24, 3)
+    g = (ne / 1e24 - 1) / 0.2
+    assert abs(g.mean()) < 1e-3 and abs(g.std() - 1) < 2e-2
+    F = R.grf_spectrum_half(16, 1.0, -3.0, 9)
+    full = np.fft.irfftn(F, s=(16, 16, 16), axes=(0, 1, 2))
+    assert np.isfinite(full).all()

@@ -1,0 +1,291 @@
+"""Device-level API: one function per libturbotrace entry point.
+
+Inputs and outputs are torch CUDA tensors (torch owns every buffer: outputs
+and scratch are allocated here and handed to the C ABI as raw pointers).
+Work is enqueued on ``torch.cuda.current_stream()``; nothing here
+synchronises the host except ``tt_volume_plan`` (pure host arithmetic) and
+the FP64 calc_dndr omega (returned through a host scalar).
+
+There is no CPU path: every function raises when CUDA or the library is
+unavailable.
+"""
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check
+
+C_LIGHT = 299792458.0
+
+
+def require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("turbulence_tracing_gb300 needs a CUDA GPU (sm_103a); none is available")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _f64_dev(a, dev):
+    if isinstance(a, torch.Tensor):
+        return a.to(device=dev, dtype=torch.float64).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=dev)
+
+
+def _dens_dev(ne, dev):
+    """Density to the device, keeping float32 as float32 and everything else float64."""
+    if isinstance(ne, torch.Tensor):
+        t = ne.to(device=dev)
+        if t.dtype not in (torch.float32, torch.float64):
+            t = t.to(torch.float64)
+        return t.contiguous()
+    a = np.asarray(ne)
+    if a.dtype == np.float32:
+        return torch.as_tensor(np.ascontiguousarray(a), device=dev)
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=dev)
+
+
+def _dtype_code(t):
+    return _lib.TT_F32 if t.dtype == torch.float32 else _lib.TT_F64
+
+
+def workspace(nbytes, dev):
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=dev)
+
+
+# ---------------------------------------------------------------------------
+# K1
+# ---------------------------------------------------------------------------
+def calc_dndr(ne, x, y, z, lwl=1053e-9, ne_max=1.0):
+    """FP64 calc_dndr on the GPU.  Returns dict(omega, ne_nc, dndx, dndy, dndz)
+    of device tensors shaped like ne (bit-identical to numpy)."""
+    dev = require_cuda()
+    L = _lib.lib()
+    ne_t = _dens_dev(ne, dev)
+    if ne_t.dim() != 3:
+        raise ValueError("ne must be a 3D array (nx, ny, nz)")
+    nx, ny, nz = ne_t.shape
+    xs, ys, zs = _f64_dev(x, dev), _f64_dev(y, dev), _f64_dev(z, dev)
+    if (xs.numel(), ys.numel(), zs.numel()) != (nx, ny, nz):
+        raise ValueError("coordinate lengths %s do not match ne.shape %s"
+                         % ((xs.numel(), ys.numel(), zs.numel()), tuple(ne_t.shape)))
+    out = {k: torch.empty((nx, ny, nz), dtype=torch.float64, device=dev) for k in ("ne_nc", "dndx", "dndy", "dndz")}
+    ws = workspace(L.tt_calc_dndr_workspace_bytes(nx, ny, nz), dev)
+    omega = ctypes.c_double(0.0)
+    check(L.tt_calc_dndr(_ptr(ne_t), _dtype_code(ne_t), nx, ny, nz, _ptr(xs), _ptr(ys), _ptr(zs), float(lwl),
+                         float(ne_max), _ptr(out["ne_nc"]), _ptr(out["dndx"]), _ptr(out["dndy"]),
+                         _ptr(out["dndz"]), ctypes.byref(omega), _ptr(ws), ws.numel(), _stream()),
+          "tt_calc_dndr")
+    out["omega"] = omega.value
+    out["coords"] = (xs, ys, zs)
+    out["_ws"] = ws  # keep alive until the stream has consumed it
+    return out
+
+
+def dndr(vols, coords, pts):
+    """Trilinear lookups (fill 0 outside) of up to 4 FP64 volumes at pts (3, N)."""
+    dev = require_cuda()
+    L = _lib.lib()
+    pts_t = _f64_dev(pts, dev)
+    if pts_t.dim() != 2 or pts_t.shape[0] != 3:
+        raise ValueError("pts must be (3, N)")
+    n = pts_t.shape[1]
+    nx, ny, nz = vols[0].shape
+    out = torch.empty((len(vols), n), dtype=torch.float64, device=dev)
+    arr = (ctypes.c_void_p * len(vols))(*[v.data_ptr() for v in vols])
+    xs, ys, zs = coords
+    check(L.tt_dndr(arr, len(vols), nx, ny, nz, _ptr(xs), _ptr(ys), _ptr(zs), _ptr(pts_t), n, _ptr(out),
+                    _stream()), "tt_dndr")
+    return out
+
+
+def volume_plan(shape, x, y, z, probing_axis, lwl, ne_max=1.0):
+    L = _lib.lib()
+    vol = _lib.TTVolume()
+    xa, ya, za = (np.ascontiguousarray(np.asarray(c, dtype=np.float64)) for c in (x, y, z))
+    dp = ctypes.POINTER(ctypes.c_double)
+    check(L.tt_volume_plan(shape[0], shape[1], shape[2], xa.ctypes.data_as(dp), ya.ctypes.data_as(dp),
+                           za.ctypes.data_as(dp), int(probing_axis), float(lwl), float(ne_max),
+                           ctypes.byref(vol)), "tt_volume_plan")
+    return vol
+
+
+class Volume32:
+    """FP32 brick volume: the tt_volume descriptor plus the torch tensor holding its nodes."""
+
+    def __init__(self, desc, nodes):
+        self.desc = desc
+        self.nodes = nodes
+
+    @property
+    def nbytes(self):
+        return self.nodes.numel() * self.nodes.element_size()
+
+
+def build_volume(ne, x, y, z, probing_axis=2, lwl=1053e-9, ne_max=1.0):
+    """K1 FP32: write the brick-tiled node volume from a density (numpy or tensor)."""
+    dev = require_cuda()
+    L = _lib.lib()
+    ne_t = _dens_dev(ne, dev)
+    desc = volume_plan(tuple(ne_t.shape), x, y, z, probing_axis, lwl, ne_max)
+    nodes = torch.empty((desc.n_float4, 4), dtype=torch.float32, device=dev)
+    desc.nodes = nodes.data_ptr()
+    check(L.tt_volume_build(ctypes.byref(desc), _ptr(ne_t), _dtype_code(ne_t), _stream()), "tt_volume_build")
+    return Volume32(desc, nodes)
+
+
+# ---------------------------------------------------------------------------
+# K2
+# ---------------------------------------------------------------------------
+def _opts(rtol, atol, atol_phase, max_steps, with_phase):
+    o = _lib.TTTraceOpts()
+    o.rtol = float(rtol)
+    o.atol = float(atol)
+    o.atol_phase = float(atol_phase)
+    o.max_steps = int(max_steps or 0)
+    o.with_phase = 1 if with_phase else 0
+    return o
+
+
+def _ray_outputs(np_, dev, want_sf=True):
+    return dict(sf=torch.empty((6, np_), dtype=torch.float64, device=dev) if want_sf else None,
+                rf=torch.empty((4, np_), dtype=torch.float64, device=dev),
+                phase=torch.empty((np_,), dtype=torch.float64, device=dev),
+                status=torch.empty((np_,), dtype=torch.int32, device=dev),
+                nsteps=torch.empty((np_,), dtype=torch.int32, device=dev))
+
+
+def trace_f64(fields, s0, t_end, probing_axis, extent, rtol=1e-3, atol=1e-6, phase=False, max_steps=None):
+    """Plain FP64 drop-in tracer.  fields: dict from calc_dndr.  s0: (6, Np)."""
+    dev = require_cuda()
+    L = _lib.lib()
+    s0_t = _f64_dev(s0, dev)
+    if s0_t.dim() != 2 or s0_t.shape[0] != 6:
+        raise ValueError("s0 must be (6, Np)")
+    np_ = s0_t.shape[1]
+    out = _ray_outputs(np_, dev)
+    nx, ny, nz = fields["dndx"].shape
+    xs, ys, zs = fields["coords"]
+    o = _opts(rtol, atol, 0.0, max_steps, phase)
+    check(L.tt_trace_f64(_ptr(fields["dndx"]), _ptr(fields["dndy"]), _ptr(fields["dndz"]), _ptr(fields["ne_nc"]),
+                         nx, ny, nz, _ptr(xs), _ptr(ys), _ptr(zs), float(fields["omega"]), _ptr(s0_t), np_,
+                         float(t_end), int(probing_axis), float(extent), ctypes.byref(o), _ptr(out["sf"]),
+                         _ptr(out["rf"]), _ptr(out["phase"]), _ptr(out["status"]), _ptr(out["nsteps"]),
+                         _stream()), "tt_trace_f64")
+    return out
+
+
+def trace_f32(vol, s0, t_end, extent, rtol=1e-6, atol=1e-5, atol_phase=1e-5, phase=False, max_steps=None,
+              want_sf=True, ws=None, out=None):
+    """Persistent FP32 tracer over a Volume32.  s0: (6, Np) float64."""
+    dev = require_cuda()
+    L = _lib.lib()
+    s0_t = _f64_dev(s0, dev)
+    if s0_t.dim() != 2 or s0_t.shape[0] != 6:
+        raise ValueError("s0 must be (6, Np)")
+    np_ = s0_t.shape[1]
+    if out is None:
+        out = _ray_outputs(np_, dev, want_sf)
+    need = L.tt_trace_f32_workspace_bytes(ctypes.byref(vol.desc), np_)
+    if ws is None or ws.numel() < need:
+        ws = workspace(need, dev)
+    o = _opts(rtol, atol, atol_phase, max_steps, phase)
+    check(L.tt_trace_f32(ctypes.byref(vol.desc), _ptr(s0_t), np_, float(t_end), float(extent), ctypes.byref(o),
+                         _ptr(out["sf"]), _ptr(out["rf"]), _ptr(out["phase"]) if phase else None,
+                         _ptr(out["status"]), _ptr(out["nsteps"]), _ptr(ws), ws.numel(), _stream()),
+          "tt_trace_f32")
+    out["_ws"] = ws
+    return out
+
+
+# ---------------------------------------------------------------------------
+# K3
+# ---------------------------------------------------------------------------
+def make_chain(ops):
+    """ops: list of (kind, p0, p1, p2) tuples -> ctypes array of tt_optic."""
+    if len(ops) > _lib.MAX_OPTICS:
+        raise ValueError("at most %d optics per chain" % _lib.MAX_OPTICS)
+    arr = (_lib.TTOptic * max(len(ops), 1))()
+    for i, op in enumerate(ops):
+        arr[i].kind = int(op[0])
+        for k, v in enumerate(op[1:4]):
+            arr[i].p[k] = float(v)
+    return arr, len(ops)
+
+
+def detect(rf, ops, nbx=1, nby=1, xr=(-1.0, 1.0), yr=(-1.0, 1.0), weights=None, H=None, Hw=None, r_out=False,
+           accumulate=False, histogram=True):
+    """Push rf (4, N) through the optic chain and (unless histogram=False)
+    histogram it.  Returns (H, Hw, r_out) device tensors; H is (nby, nbx) like Rays.H."""
+    dev = require_cuda()
+    L = _lib.lib()
+    rf_t = _f64_dev(rf, dev)
+    if rf_t.dim() != 2 or rf_t.shape[0] != 4:
+        raise ValueError("rf must be (4, N)")
+    n = rf_t.shape[1]
+    if histogram and H is None:
+        H = torch.empty((nby, nbx), dtype=torch.float64, device=dev)
+    w_t = _f64_dev(weights, dev) if weights is not None else None
+    if not histogram:
+        H, w_t = None, None
+    if w_t is not None and Hw is None:
+        Hw = torch.empty((nby, nbx), dtype=torch.float64, device=dev)
+    ro = torch.empty((4, n), dtype=torch.float64, device=dev) if r_out else None
+    chain, nops = make_chain(ops)
+    check(L.tt_detect(_ptr(rf_t), n, chain, nops, int(nbx), int(nby), float(xr[0]), float(xr[1]),
+                      float(yr[0]), float(yr[1]), _ptr(w_t), _ptr(H), _ptr(Hw) if w_t is not None else None,
+                      _ptr(ro), 1 if accumulate else 0, _stream()), "tt_detect")
+    return H, (Hw if w_t is not None else None), ro
+
+
+# ---------------------------------------------------------------------------
+# K4
+# ---------------------------------------------------------------------------
+def grf_field(n, L_box, alpha, ne0, delta, seed, dtype=torch.float32, kmin=None, kmax=None):
+    """Band-limited unit-variance GRF density ne0 (1 + delta g) clipped >= 0, (n, n, n)."""
+    dev = require_cuda()
+    L = _lib.lib()
+    kmin = 2 * math.pi / L_box if kmin is None else kmin
+    kmax = math.pi * n / L_box if kmax is None else kmax
+    out = torch.empty((n, n, n), dtype=dtype, device=dev)
+    ws = workspace(L.tt_grf_field_workspace_bytes(n), dev)
+    code = _lib.TT_F32 if dtype == torch.float32 else _lib.TT_F64
+    check(L.tt_grf_field(int(seed) & 0xFFFFFFFFFFFFFFFF, n, float(L_box), float(alpha), float(kmin), float(kmax),
+                         float(ne0), float(delta), code, _ptr(out), _ptr(ws), ws.numel(), _stream()),
+          "tt_grf_field")
+    del ws
+    return out
+
+
+def grf_fft(N, sqrt_p_half, seed=0, Wr=None, Wi=None):
+    """gaussian3D_FFT core: sqrt_p_half (M, M, N+1) device float64."""
+    dev = require_cuda()
+    L = _lib.lib()
+    M = 2 * N + 1
+    sp = _f64_dev(sqrt_p_half, dev)
+    if tuple(sp.shape) != (M, M, N + 1):
+        raise ValueError("sqrt_p_half must be (M, M, N+1)")
+    wr = _f64_dev(Wr, dev) if Wr is not None else None
+    wi = _f64_dev(Wi, dev) if Wi is not None else None
+    out = torch.empty((M, M, M), dtype=torch.float64, device=dev)
+    ws = workspace(L.tt_grf_fft_workspace_bytes(N), dev)
+    check(L.tt_grf_fft(int(seed) & 0xFFFFFFFFFFFFFFFF, N, _ptr(sp), _ptr(wr), _ptr(wi), _ptr(out), _ptr(ws),
+                       ws.numel(), _stream()), "tt_grf_fft")
+    return out
+
+
+def philox(seed, tag, count):
+    dev = require_cuda()
+    out = torch.empty((4, count), dtype=torch.int32, device=dev)
+    check(_lib.lib().tt_philox(int(seed) & 0xFFFFFFFFFFFFFFFF, int(tag) & 0xFFFFFFFF, int(count), _ptr(out),
+                               _stream()), "tt_philox")
+    return out

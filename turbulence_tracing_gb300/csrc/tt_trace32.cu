@@ -1,0 +1,708 @@
+// K2b: persistent FP32 tracer over the brick-tiled node volume.
+//
+// Same ODE as ElectronCube.solve/dsdt/dndr (particle_tracking/particle_tracker.py:
+// 243-256, 312-331, 398-419) in normalised variables:
+//   P  = position in cells along (a, b, c), kept as integer cell + fraction,
+//   u  = v / c,  sigma = c t / spacing_c (path parameter in cells of the probing axis),
+//   dP/dsigma = r u   (r = spacing_c / spacing_axis),
+//   du/dsigma = H(P)  (H = -0.5 d(ne_nc)/dx * spacing_c, trilinear in the cell),
+//   dphi/dsigma = kappa (n - 1) |u|, n - 1 = -q / (1 + sqrt(1 - q)), kappa = k0 spacing_c.
+// Each Dormand-Prince 5(4) step is clipped to end just past the next cell face,
+// so all seven stages evaluate one cell's trilinear polynomial (loaded once,
+// 8 float4 nodes) and the step never straddles a kink of the interpolant.
+// The face of the box is hit exactly (the field jumps to 0 outside, as
+// RegularGridInterpolator's fill_value=0).  Outside the box the ray is a
+// straight line, finished analytically.  Error control per ray (scipy's
+// controller constants) on position (cells), velocity and phase.
+// Position fraction, path length and phase are compensated sums.
+//
+// Work distribution: rays are bucketed by the 4x4-cell tile they start in
+// (Morton order inside 8x8 super-tiles, the volume's own tile order), then a
+// persistent grid (one wave of resident blocks) pulls rays from that order
+// through a global work counter; each warp refills its finished lanes with one
+// warp-aggregated atomic (ballot / popc), so lanes stay busy while rays with
+// long and short paths mix.
+#include <math.h>
+
+#include "tt_common.cuh"
+
+namespace {
+
+__device__ __host__ inline uint32_t spread3(uint32_t v)
+{
+    return (v & 1u) | ((v & 2u) << 1) | ((v & 4u) << 2);
+}
+
+struct Tab {
+    float cs[7];
+    float a[7][6];   // row 6 = b
+    float aa[7][6];  // (A A)[s][k]
+    float e[7];
+    float ea[6];     // sum_j e_j a[j][k] with a[6] = b
+    float b[6];
+};
+
+Tab make_tab()
+{
+    const double C[7] = {0.0, 1.0 / 5, 3.0 / 10, 4.0 / 5, 8.0 / 9, 1.0, 1.0};
+    double A[7][6] = {{0}};
+    const double Ar[6][5] = {
+        {0, 0, 0, 0, 0},
+        {1.0 / 5, 0, 0, 0, 0},
+        {3.0 / 40, 9.0 / 40, 0, 0, 0},
+        {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0},
+        {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0},
+        {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656}};
+    const double B[6] = {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84};
+    const double E[7] = {-71.0 / 57600, 0, 71.0 / 16695, -71.0 / 1920, 17253.0 / 339200, -22.0 / 525, 1.0 / 40};
+    for (int s = 0; s < 6; ++s)
+        for (int k = 0; k < 5; ++k) A[s][k] = Ar[s][k];
+    for (int k = 0; k < 6; ++k) A[6][k] = B[k];
+    Tab t;
+    for (int s = 0; s < 7; ++s) {
+        t.cs[s] = (float)C[s];
+        t.e[s] = (float)E[s];
+        for (int k = 0; k < 6; ++k) {
+            t.a[s][k] = (float)A[s][k];
+            double acc = 0.0;
+            for (int j = 0; j < 6; ++j) acc += A[s][j] * A[j][k];
+            t.aa[s][k] = (float)acc;
+        }
+    }
+    for (int k = 0; k < 6; ++k) {
+        double acc = 0.0;
+        for (int j = 0; j < 7; ++j) acc += E[j] * A[j][k];
+        t.ea[k] = (float)acc;
+        t.b[k] = (float)B[k];
+    }
+    return t;
+}
+
+struct Vol32 {
+    const float4* __restrict__ nodes;
+    int n[3];
+    int st_b;
+    long long tile_f4;
+    float r[3];
+    double origin[3];
+    double spacing[3];
+    int axis[3];
+    float kappa;
+    double sig_end;
+    double t_end;
+    double extent;
+    float rtol, atol_cells, atol_phase;
+    int with_phase;
+    long long max_steps;
+};
+
+__device__ inline long long tile_base(const Vol32& V, int ta, int tb)
+{
+    const int sa = ta >> 3, sb = tb >> 3;
+    const uint32_t m = spread3((uint32_t)(ta & 7)) | (spread3((uint32_t)(tb & 7)) << 1);
+    return ((long long)(sa * V.st_b + sb) * 64 + m) * V.tile_f4;
+}
+
+__device__ inline int tile_key(const Vol32& V, int ta, int tb)
+{
+    const int sa = ta >> 3, sb = tb >> 3;
+    const uint32_t m = spread3((uint32_t)(ta & 7)) | (spread3((uint32_t)(tb & 7)) << 1);
+    return (sa * V.st_b + sb) * 64 + (int)m;
+}
+
+__device__ __forceinline__ float tri(const float* c, float fa, float fb, float fc)
+{
+    const float t1 = fmaf(c[7], fc, c[4]);
+    const float t2 = fmaf(c[5], fc, c[1]);
+    const float t3 = fmaf(fb, t1, t2);
+    const float t4 = fmaf(c[6], fc, c[2]);
+    const float t5 = fmaf(c[3], fc, c[0]);
+    const float t6 = fmaf(fb, t4, t5);
+    return fmaf(fa, t3, t6);
+}
+
+// Polynomial coefficients of the trilinear interpolant of one component.
+__device__ __forceinline__ void poly(float v000, float v001, float v010, float v011, float v100, float v101,
+                            float v110, float v111, float* c)
+{
+    c[0] = v000;
+    c[1] = v100 - v000;
+    c[2] = v010 - v000;
+    c[3] = v001 - v000;
+    c[4] = (v110 - v100) - (v010 - v000);
+    c[5] = (v101 - v100) - (v001 - v000);
+    c[6] = (v011 - v010) - (v001 - v000);
+    c[7] = ((v111 - v110) - (v101 - v100)) - ((v011 - v010) - (v001 - v000));
+}
+
+__device__ __forceinline__ void load_cell(const Vol32& V, long long tbase, int ca, int cb, int cc, float (*coef)[8])
+{
+    const long long base = tbase + (long long)(cc >> 3) * 200 + ((ca & 3) * 5 + (cb & 3)) * 8 + (cc & 7);
+    const int dc = ((cc & 7) == 7) ? 193 : 1;
+    const float4* p = V.nodes + base;
+    const float4 n000 = __ldg(p), n001 = __ldg(p + dc);
+    const float4 n010 = __ldg(p + 8), n011 = __ldg(p + 8 + dc);
+    const float4 n100 = __ldg(p + 40), n101 = __ldg(p + 40 + dc);
+    const float4 n110 = __ldg(p + 48), n111 = __ldg(p + 48 + dc);
+    poly(n000.x, n001.x, n010.x, n011.x, n100.x, n101.x, n110.x, n111.x, coef[0]);
+    poly(n000.y, n001.y, n010.y, n011.y, n100.y, n101.y, n110.y, n111.y, coef[1]);
+    poly(n000.z, n001.z, n010.z, n011.z, n100.z, n101.z, n110.z, n111.z, coef[2]);
+    poly(n000.w, n001.w, n010.w, n011.w, n100.w, n101.w, n110.w, n111.w, coef[3]);
+}
+
+__device__ inline float nm1f(float q)
+{
+    float r = 1.0f - q;
+    r = r > 0.0f ? r : 0.0f;
+    return -q / (1.0f + sqrtf(r));
+}
+
+// Neumaier summation s + x with running compensation c (no contraction).
+__device__ inline void neumaier(float& s, float& c, float x)
+{
+    const float t = __fadd_rn(s, x);
+    if (fabsf(s) >= fabsf(x)) c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, t), x));
+    else c = __fadd_rn(c, __fadd_rn(__fsub_rn(x, t), s));
+    s = t;
+}
+
+struct Ray {
+    int ci[3];
+    float fr[3];
+    float u[3];
+    float sig, sigc;
+    float ph, phc;
+    float hctrl;
+    int natt, nacc;
+    int state;     // 0 = stepping, 1 = exited box, 2 = reached sigma_end, 3 = failed
+    int code;
+    bool rejected;
+    bool cell_dirty;
+    bool entered;
+    int ta, tb;
+    long long tbase;
+};
+
+constexpr float kFaceEps = 1e-3f;    // aim this far (cells) past an interior face
+constexpr float kBoxSnap = 1e-5f;    // closer than this to the box face, moving out: exited
+
+__device__ __forceinline__ bool outside_cell(const Vol32& V, Ray& R)
+{
+    // normalise: P = ci + fr with fr in [0, 1); the upper box face belongs to the last cell
+    bool out = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float fl = floorf(R.fr[a]);
+        if (fl != 0.0f) {
+            R.ci[a] += (int)fl;
+            R.fr[a] -= fl;
+            R.cell_dirty = true;
+        }
+        if (R.ci[a] == V.n[a] - 1 && R.fr[a] == 0.0f) {
+            R.ci[a] = V.n[a] - 2;
+            R.fr[a] = 1.0f;
+        }
+        if (R.ci[a] < 0 || R.ci[a] > V.n[a] - 2) out = true;
+    }
+    return out;
+}
+
+// Initialise from s0 (SI units, physical axes).  Returns false when the ray
+// never enters the box before t_end (straight line throughout).
+__device__ __forceinline__ bool init_ray(const Vol32& V, const double* __restrict__ s0, long long np, long long r, Ray& R,
+                         double P[3], double uu[3])
+{
+    double x[3], v[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        x[i] = s0[(size_t)i * np + r];
+        v[i] = s0[(size_t)(3 + i) * np + r];
+    }
+    bool finite = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        P[a] = (x[V.axis[a]] - V.origin[a]) / V.spacing[a];
+        // a start on a box face (up to the rounding of this transform) is on it,
+        // as RegularGridInterpolator counts the end coordinates as inside
+        const double hi = (double)(V.n[a] - 1);
+        if (fabs(P[a]) < 1e-9) P[a] = 0.0;
+        if (fabs(P[a] - hi) < 1e-9 * hi) P[a] = hi;
+        uu[a] = v[V.axis[a]] / TT_C_LIGHT;
+        finite = finite && isfinite(P[a]) && isfinite(uu[a]);
+    }
+    R.natt = R.nacc = 0;
+    R.sig = R.sigc = 0.f;
+    R.ph = R.phc = 0.f;
+    R.hctrl = 1.0f;
+    R.rejected = false;
+    R.entered = false;
+    R.code = TT_RAY_OK;
+    if (!finite) {
+        R.code = TT_RAY_NAN;
+        R.state = 3;
+        return false;
+    }
+    // slab test in sigma units: dP/dsigma = r u
+    double tin = 0.0, tout = V.sig_end;
+    int enter_axis = -1;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double vel = (double)V.r[a] * uu[a];
+        const double hi = (double)(V.n[a] - 1);
+        if (vel == 0.0) {
+            if (P[a] < 0.0 || P[a] > hi) tout = -1.0;
+        } else {
+            double t1 = (0.0 - P[a]) / vel, t2 = (hi - P[a]) / vel;
+            if (t1 > t2) { const double t = t1; t1 = t2; t2 = t; }
+            if (t1 > tin) { tin = t1; enter_axis = a; }
+            if (t2 < tout) tout = t2;
+        }
+    }
+    if (!(tin <= tout) || tin >= V.sig_end) {
+        R.state = 1;  // never inside: straight line
+        R.sig = 0.f;
+        return false;
+    }
+    double Pe[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) Pe[a] = P[a] + (double)V.r[a] * uu[a] * tin;
+    if (enter_axis >= 0) {
+        const double vel = (double)V.r[enter_axis] * uu[enter_axis];
+        Pe[enter_axis] = vel > 0 ? 0.0 : (double)(V.n[enter_axis] - 1);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double c = floor(Pe[a]);
+        if (c > V.n[a] - 2) c = V.n[a] - 2;
+        if (c < 0) c = 0;
+        R.ci[a] = (int)c;
+        R.fr[a] = (float)(Pe[a] - c);
+        R.u[a] = (float)uu[a];
+    }
+    R.sig = (float)tin;
+    R.sigc = (float)(tin - (double)R.sig);
+    R.state = 0;
+    R.entered = true;
+    R.cell_dirty = true;
+    R.ta = -1;
+    R.tb = -1;
+    return true;
+}
+
+__device__ __forceinline__ void finish_ray(const Vol32& V, const Ray& R, const double P0[3], const double u0[3], long long r,
+                           long long np, double* __restrict__ sf, double* __restrict__ rf,
+                           double* __restrict__ phase, int* __restrict__ status, int* __restrict__ nsteps)
+{
+    // Position/velocity where stepping stopped, then the straight-line flight to
+    // t_end for rays outside the box (zero field there): rays that left the box,
+    // and rays that never meet it (whole interval).
+    double P[3], u[3], ds = 0.0;
+    if (R.entered) {
+        const double sig = (double)R.sig + (double)R.sigc;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            P[a] = (double)R.ci[a] + (double)R.fr[a];
+            u[a] = (double)R.u[a];
+        }
+        if (R.state == 1 && R.code == TT_RAY_OK) ds = V.sig_end - sig > 0.0 ? V.sig_end - sig : 0.0;
+    } else {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            P[a] = P0[a];
+            u[a] = u0[a];
+        }
+        if (R.code == TT_RAY_OK) ds = V.sig_end;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) P[a] += (double)V.r[a] * u[a] * ds;
+    double y[6];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        y[V.axis[a]] = V.origin[a] + P[a] * V.spacing[a];
+        y[3 + V.axis[a]] = u[a] * TT_C_LIGHT;
+    }
+    if (sf) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) sf[(size_t)i * np + r] = y[i];
+    }
+    if (rf) {
+        const int ax = V.axis[2];
+        const int p0 = ax == 0 ? 1 : 0, p1 = ax == 2 ? 1 : 2;
+        const double tbp = (y[ax] - V.extent) / y[3 + ax];
+        rf[r] = y[p0] - y[3 + p0] * tbp;
+        rf[(size_t)2 * np + r] = y[p1] - y[3 + p1] * tbp;
+        rf[(size_t)np + r] = atan(y[3 + p0] / y[3 + ax]);
+        rf[(size_t)3 * np + r] = atan(y[3 + p1] / y[3 + ax]);
+    }
+    if (phase) phase[r] = (double)R.ph + (double)R.phc;
+    if (status) status[r] = R.code;
+    if (nsteps) nsteps[r] = R.nacc;
+}
+
+// One attempted step.  Returns with R updated.
+__device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float (*coef)[8])
+{
+    if (R.cell_dirty) {
+        const int ta = R.ci[0] >> 2, tb = R.ci[1] >> 2;
+        if (ta != R.ta || tb != R.tb) {
+            R.ta = ta;
+            R.tb = tb;
+            R.tbase = tile_base(V, ta, tb);
+        }
+        load_cell(V, R.tbase, R.ci[0], R.ci[1], R.ci[2], coef);
+        R.cell_dirty = false;
+    }
+    // distance to the faces of the current cell along the ray
+    float hf = 3.0e38f;
+    bool at_box_face = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float vel = V.r[a] * R.u[a];
+        if (vel > 0.f) {
+            const bool boxf = R.ci[a] == V.n[a] - 2;
+            const float d = 1.0f - R.fr[a];
+            if (boxf && d < kBoxSnap) at_box_face = true;
+            hf = fminf(hf, (d + (boxf ? 0.f : kFaceEps)) / vel);
+        } else if (vel < 0.f) {
+            const bool boxf = R.ci[a] == 0;
+            const float d = R.fr[a];
+            if (boxf && d < kBoxSnap) at_box_face = true;
+            hf = fminf(hf, (d + (boxf ? 0.f : kFaceEps)) / (-vel));
+        }
+    }
+    if (at_box_face) {
+        R.state = 1;
+        return;
+    }
+    const float rem = (float)(V.sig_end - ((double)R.sig + (double)R.sigc));
+    if (!(rem > 0.f)) {
+        R.state = 2;
+        return;
+    }
+    if (R.natt >= V.max_steps) {
+        R.code = TT_RAY_MAX_STEPS;
+        R.state = 3;
+        return;
+    }
+    ++R.natt;
+    bool last = false;
+    float h = fminf(R.hctrl, hf);
+    if (h >= rem) {
+        h = rem;
+        last = true;
+    }
+    // Stages: store H_k (3 comps); accumulate phase sums on the fly.
+    float Hs[7][3];
+    float phb = 0.f, phe = 0.f;
+    float Pn[3], un[3];
+#pragma unroll
+    for (int s = 0; s < 7; ++s) {
+        float Ps[3], us[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            float sa = 0.f, saa = 0.f;
+#pragma unroll
+            for (int k = 0; k < s && k < 6; ++k) {
+                sa = fmaf(T.a[s][k], Hs[k][c], sa);
+                saa = fmaf(T.aa[s][k], Hs[k][c], saa);
+            }
+            us[c] = fmaf(h, sa, R.u[c]);
+            Ps[c] = fmaf(h * V.r[c], fmaf(T.cs[s], R.u[c], h * saa), R.fr[c]);
+        }
+        Hs[s][0] = tri(coef[0], Ps[0], Ps[1], Ps[2]);
+        Hs[s][1] = tri(coef[1], Ps[0], Ps[1], Ps[2]);
+        Hs[s][2] = tri(coef[2], Ps[0], Ps[1], Ps[2]);
+        if (V.with_phase) {
+            const float q = tri(coef[3], Ps[0], Ps[1], Ps[2]);
+            const float sp = sqrtf(fmaf(us[0], us[0], fmaf(us[1], us[1], us[2] * us[2])));
+            const float dph = V.kappa * nm1f(q) * sp;
+            if (s < 6) phb = fmaf(T.b[s], dph, phb);
+            phe = fmaf(T.e[s], dph, phe);
+        }
+        if (s == 6) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                Pn[c] = Ps[c];
+                un[c] = us[c];
+            }
+        }
+    }
+    // error estimate; velocity scale is rtol times the speed (|u| ~ 1), so the
+    // velocity tolerance is an angle
+    const float sp0 = sqrtf(fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2])));
+    const float sp1 = sqrtf(fmaf(un[0], un[0], fmaf(un[1], un[1], un[2] * un[2])));
+    const float scu = V.rtol * fmaxf(sp0, sp1) + 1e-30f;
+    float es = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float eu = 0.f, ep = 0.f;
+#pragma unroll
+        for (int k = 0; k < 7; ++k) eu = fmaf(T.e[k], Hs[k][c], eu);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) ep = fmaf(T.ea[k], Hs[k][c], ep);
+        eu *= h;
+        ep *= h * h * V.r[c];
+        const float x1 = eu / scu;
+        const float x2 = ep / V.atol_cells;
+        es = fmaf(x1, x1, fmaf(x2, x2, es));
+    }
+    int neq = 6;
+    float dphi = 0.f;
+    if (V.with_phase) {
+        dphi = h * phb;
+        const float phn = R.ph + dphi;
+        const float scp = V.atol_phase + V.rtol * fmaxf(fabsf(R.ph), fabsf(phn));
+        const float x = h * phe / scp;
+        es = fmaf(x, x, es);
+        neq = 7;
+    }
+    const float en = sqrtf(es / (float)neq);
+    if (en < 1.0f || !(en == en)) {
+        if (!(en == en)) {
+            R.code = TT_RAY_NAN;
+            R.state = 3;
+            return;
+        }
+        float factor = en == 0.f ? 10.f : fminf(10.f, 0.9f * __powf(en, -0.2f));
+        if (R.rejected) factor = fminf(1.f, factor);
+        R.rejected = false;
+        R.hctrl = h * factor;
+        ++R.nacc;
+        // commit
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            R.fr[c] = Pn[c];
+            R.u[c] = un[c];
+        }
+        {  // Kahan on sigma
+            const float y = __fsub_rn(h, R.sigc);
+            const float t = __fadd_rn(R.sig, y);
+            R.sigc = __fsub_rn(__fsub_rn(t, R.sig), y);
+            R.sig = t;
+        }
+        if (V.with_phase) neumaier(R.ph, R.phc, dphi);
+        const bool out = outside_cell(V, R);
+        if (out) R.state = 1;
+        else if (last) R.state = 2;
+    } else {
+        float factor = fmaxf(0.2f, 0.9f * __powf(en, -0.2f));
+        R.hctrl = h * factor;
+        R.rejected = true;
+        if (R.hctrl < 1e-7f) {
+            R.code = TT_RAY_STEP_TOO_SMALL;
+            R.state = 3;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128, 4)
+trace32_kernel(Vol32 V, Tab T, const double* __restrict__ s0, long long np,
+               const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
+               double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
+               int* __restrict__ status, int* __restrict__ nsteps)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    long long idx = -1;      // position in perm of this lane's ray
+    bool drained = false;
+    Ray R;
+    double P0[3], u0[3];
+    float coef[4][8];
+    R.state = 1;
+    for (;;) {
+        const bool need = (idx < 0) && !drained;
+        const unsigned mask = __ballot_sync(0xffffffffu, need);
+        if (mask) {
+            unsigned long long base = 0;
+            const int leader = __ffs(mask) - 1;
+            if ((int)lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                const unsigned long long my = base + __popc(mask & ((1u << lane) - 1u));
+                if (my < (unsigned long long)np) {
+                    idx = (long long)my;
+                    const long long r = perm ? (long long)perm[idx] : idx;
+                    if (!init_ray(V, s0, np, r, R, P0, u0)) {
+                        finish_ray(V, R, P0, u0, r, np, sf, rf, phase, status, nsteps);
+                        idx = -1;  // picked up again on the next pass
+                    }
+                } else {
+                    drained = true;
+                }
+            }
+        }
+        const bool active = idx >= 0;
+        if (__ballot_sync(0xffffffffu, active || (!drained)) == 0u) break;
+        if (active) {
+            step(V, T, R, coef);
+            if (R.state != 0) {
+                const long long r = perm ? (long long)perm[idx] : idx;
+                finish_ray(V, R, P0, u0, r, np, sf, rf, phase, status, nsteps);
+                idx = -1;
+            }
+        }
+    }
+}
+
+// --- ray bucketing by entry tile ----------------------------------------------
+__device__ inline int ray_key(const Vol32& V, const double* __restrict__ s0, long long np, long long r)
+{
+    const double xa = s0[(size_t)V.axis[0] * np + r];
+    const double xb = s0[(size_t)V.axis[1] * np + r];
+    double pa = (xa - V.origin[0]) / V.spacing[0];
+    double pb = (xb - V.origin[1]) / V.spacing[1];
+    if (!(pa >= 0.0)) pa = 0.0;  // NaN too
+    if (!(pb >= 0.0)) pb = 0.0;
+    int ca = pa > (double)(V.n[0] - 2) ? V.n[0] - 2 : (int)pa;
+    int cb = pb > (double)(V.n[1] - 2) ? V.n[1] - 2 : (int)pb;
+    return tile_key(V, ca >> 2, cb >> 2);
+}
+
+__global__ void bin_count_kernel(Vol32 V, const double* __restrict__ s0, long long np, unsigned* __restrict__ cnt)
+{
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < np;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int key = ray_key(V, s0, np, r);
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        const int leader = __ffs(peers) - 1;
+        if ((int)(threadIdx.x & 31u) == leader) atomicAdd(cnt + key, (unsigned)__popc(peers));
+    }
+}
+
+// exclusive scan of n counters by one block (n up to a few hundred thousand)
+__global__ void bin_scan_kernel(unsigned* __restrict__ cnt, int n)
+{
+    __shared__ unsigned part[1024];
+    const int t = threadIdx.x;
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int lo = t * per, hi = min(n, lo + per);
+    unsigned s = 0;
+    for (int i = lo; i < hi; ++i) s += cnt[i];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+        const unsigned v = t >= off ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    unsigned run = part[t] - s;
+    for (int i = lo; i < hi; ++i) {
+        const unsigned c = cnt[i];
+        cnt[i] = run;
+        run += c;
+    }
+}
+
+__global__ void bin_scatter_kernel(Vol32 V, const double* __restrict__ s0, long long np,
+                                   unsigned* __restrict__ cursor, unsigned* __restrict__ perm)
+{
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < np;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int key = ray_key(V, s0, np, r);
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        const int leader = __ffs(peers) - 1;
+        unsigned base = 0;
+        if ((int)(threadIdx.x & 31u) == leader) base = atomicAdd(cursor + key, (unsigned)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        const unsigned rank = __popc(peers & ((1u << (threadIdx.x & 31u)) - 1u));
+        perm[base + rank] = (unsigned)r;
+    }
+}
+
+struct WsLayout {
+    size_t counter_off, cnt_off, perm_off, total;
+    int nbins;
+};
+
+WsLayout ws_layout(const tt_volume* vol, long long np)
+{
+    WsLayout L;
+    L.nbins = vol->supertiles[0] * vol->supertiles[1] * 64;
+    L.counter_off = 0;
+    L.cnt_off = 256;
+    L.perm_off = tt::align_up(L.cnt_off + sizeof(unsigned) * (size_t)L.nbins, 256);
+    L.total = tt::align_up(L.perm_off + sizeof(unsigned) * (size_t)np, 256);
+    return L;
+}
+
+int occupancy_grid()
+{
+    static int blocks_per_sm[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int b = (dev >= 0 && dev < 64) ? blocks_per_sm[dev] : 0;
+    if (b <= 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace32_kernel, 128, 0) != cudaSuccess || b < 1)
+            b = 1;
+        if (dev >= 0 && dev < 64) blocks_per_sm[dev] = b;
+    }
+    return b * tt::sm_count();
+}
+
+}  // namespace
+
+extern "C" size_t tt_trace_f32_workspace_bytes(const tt_volume* vol, int64_t np)
+{
+    if (!vol || np < 0) return 0;
+    return ws_layout(vol, np).total;
+}
+
+extern "C" int tt_trace_f32(const tt_volume* vol, const double* s0, int64_t np, double t_end, double extent,
+                            const tt_trace_opts* opts, double* sf, double* rf, double* phase, int32_t* status,
+                            int32_t* nsteps, void* workspace, size_t workspace_bytes, void* stream)
+{
+    if (!vol || !opts) return tt::invalid("trace_f32: null volume or opts");
+    if (!vol->nodes) return tt::invalid("trace_f32: volume has no node buffer");
+    if (np < 0) return tt::invalid("trace_f32: np < 0");
+    if (np > 0xffffffffLL) return tt::invalid("trace_f32: at most 2^32-1 rays per call");
+    if (!(t_end >= 0.0)) return tt::invalid("trace_f32: t_end must be >= 0");
+    if (!(opts->rtol > 0.0) || !(opts->atol > 0.0))
+        return tt::invalid("trace_f32: need rtol > 0 and atol > 0 (cells)");
+    if (opts->with_phase && !(opts->atol_phase > 0.0)) return tt::invalid("trace_f32: need atol_phase > 0");
+    for (int i = 0; i < 3; ++i)
+        if (vol->n[i] < 2) return tt::invalid("trace_f32: volume axis with < 2 nodes");
+    if (np == 0) return TT_OK;
+    if (!s0) return tt::invalid("trace_f32: s0 is null");
+    const WsLayout L = ws_layout(vol, np);
+    if (!workspace || workspace_bytes < L.total) {
+        tt::set_detail("trace_f32: workspace needs %zu bytes", L.total);
+        return TT_ERR_WORKSPACE_TOO_SMALL;
+    }
+    static const Tab T = make_tab();
+    Vol32 V;
+    V.nodes = static_cast<const float4*>(vol->nodes);
+    for (int i = 0; i < 3; ++i) {
+        V.n[i] = vol->n[i];
+        V.origin[i] = vol->origin[i];
+        V.spacing[i] = vol->spacing[i];
+        V.axis[i] = vol->axis[i];
+        V.r[i] = (float)(vol->spacing[2] / vol->spacing[i]);
+    }
+    V.st_b = vol->supertiles[1];
+    V.tile_f4 = (long long)vol->bricks_c * 200;
+    V.kappa = (float)(vol->omega / TT_C_LIGHT * vol->spacing[2]);
+    V.sig_end = t_end * TT_C_LIGHT / vol->spacing[2];
+    V.t_end = t_end;
+    V.extent = extent;
+    V.rtol = (float)opts->rtol;
+    V.atol_cells = (float)opts->atol;
+    V.atol_phase = (float)(opts->with_phase ? opts->atol_phase : 1.0);
+    V.with_phase = opts->with_phase ? 1 : 0;
+    V.max_steps = opts->max_steps > 0 ? opts->max_steps : TT_DEFAULT_MAX_STEPS;
+
+    cudaStream_t s = tt::as_stream(stream);
+    char* ws = static_cast<char*>(workspace);
+    unsigned long long* counter = reinterpret_cast<unsigned long long*>(ws + L.counter_off);
+    unsigned* cnt = reinterpret_cast<unsigned*>(ws + L.cnt_off);
+    unsigned* perm = reinterpret_cast<unsigned*>(ws + L.perm_off);
+    TT_TRY(tt::cuda_status(cudaMemsetAsync(ws, 0, L.perm_off, s), "trace_f32 workspace clear"));
+    long long g = (np + 255) / 256;
+    const long long cap = (long long)tt::sm_count() * 16;
+    if (g > cap) g = cap;
+    bin_count_kernel<<<(int)g, 256, 0, s>>>(V, s0, np, cnt);
+    bin_scan_kernel<<<1, 1024, 0, s>>>(cnt, L.nbins);
+    bin_scatter_kernel<<<(int)g, 256, 0, s>>>(V, s0, np, cnt, perm);
+    TT_TRY(tt::launch_status("trace_f32 ray binning"));
+    trace32_kernel<<<occupancy_grid(), 128, 0, s>>>(V, T, s0, np, perm, counter, sf, rf, phase, status, nsteps);
+    return tt::launch_status("trace_f32 kernel");
+}

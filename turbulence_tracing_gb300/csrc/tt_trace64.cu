@@ -1,0 +1,423 @@
+// K2a: plain FP64 drop-in tracer and the dndr lookup.
+//
+// Replaces ElectronCube.solve / dsdt / dndr / ray_at_exit
+// (particle_tracking/particle_tracker.py:243-256, 312-380, 398-419).
+// One thread integrates one ray with its own RK45 instance that follows
+// scipy.integrate.solve_ivp(method='RK45') step for step: Dormand-Prince 5(4)
+// tableau, scipy's initial-step rule, RMS error norm over the ray's own
+// components, safety 0.9, step factors in [0.2, 10], exponent -1/5, step
+// clipped to t_bound, 10-ulp minimum step.  Lookups reproduce
+// RegularGridInterpolator(method='linear', fill_value=0) operation by
+// operation.  The file is compiled with -fmad=false so every product and sum
+// is rounded separately, as numpy does.
+//
+// The reference integrates all rays as one system with one global step; a
+// per-ray step is the GPU-natural decomposition and converges to the same
+// trajectories (parity is asserted at tight tolerance).
+#include <math.h>
+
+#include "tt_common.cuh"
+
+namespace {
+
+struct Grid64 {
+    const double* g[3];
+    int n[3];
+    size_t s0, s1;  // element strides of ix and iy
+};
+
+struct Vols64 {
+    const double* v[4];  // dndx, dndy, dndz, ne_nc
+    int nvol;
+};
+
+// searchsorted(g, v, 'left') - 1 clipped to [0, n-2], starting from a guess
+// made with the mean spacing; falls back to bisection if the guess is far off.
+__device__ inline int locate64(const double* __restrict__ g, int n, double g0, double gn, double v)
+{
+    // first guess in FP32 (the walk below makes it exact)
+    const float span = (float)(gn - g0);
+    int i = span > 0.f ? (int)floorf((float)(v - g0) * __fdividef((float)(n - 1), span)) : 0;
+    if (i < -1) i = -1;
+    if (i > n - 1) i = n - 1;
+    // want the largest i with g[i] < v (i = -1 if none)
+    int it = 0;
+    while (i + 1 < n && __ldg(g + i + 1) < v && it < 4) { ++i; ++it; }
+    while (i >= 0 && !(__ldg(g + i) < v) && it < 8) { --i; ++it; }
+    const bool ok = (i + 1 >= n || !(__ldg(g + i + 1) < v)) && (i < 0 || __ldg(g + i) < v);
+    if (!ok) {
+        int lo = 0, hi = n;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(g + mid) < v) lo = mid + 1; else hi = mid;
+        }
+        i = lo - 1;
+    }
+    if (i < 0) i = 0;
+    if (i > n - 2) i = n - 2;
+    return i;
+}
+
+// Trilinear lookup of nvol volumes at p.  Returns 0 = inside, 1 = outside
+// (values 0), 2 = NaN coordinate (values NaN).
+__device__ inline int lookup64(const Grid64& G, const Vols64& V, const double p[3], double out[4])
+{
+    int idx[3];
+    double d[3];
+    int oob = 0;
+    for (int a = 0; a < 3; ++a) {
+        const double v = p[a];
+        if (v != v) {
+            for (int k = 0; k < V.nvol; ++k) out[k] = CUDART_NAN;
+            return 2;
+        }
+        const double lo = __ldg(G.g[a]), hi = __ldg(G.g[a] + G.n[a] - 1);
+        if (v < lo || v > hi) oob = 1;
+        const int i = locate64(G.g[a], G.n[a], lo, hi, v);
+        idx[a] = i;
+        const double gi = __ldg(G.g[a] + i);
+        d[a] = (v - gi) / (__ldg(G.g[a] + i + 1) - gi);
+    }
+    if (oob) {
+        for (int k = 0; k < V.nvol; ++k) out[k] = 0.0;
+        return 1;
+    }
+    for (int k = 0; k < V.nvol; ++k) out[k] = 0.0;
+    const size_t base = (size_t)idx[0] * G.s0 + (size_t)idx[1] * G.s1 + (size_t)idx[2];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int a = c >> 2, b = (c >> 1) & 1, e = c & 1;
+        double w = 1.0;
+        w = w * (a ? d[0] : 1.0 - d[0]);
+        w = w * (b ? d[1] : 1.0 - d[1]);
+        w = w * (e ? d[2] : 1.0 - d[2]);
+        const size_t off = base + (a ? G.s0 : 0) + (b ? G.s1 : 0) + (size_t)e;
+        for (int k = 0; k < V.nvol; ++k) out[k] = out[k] + __ldg(V.v[k] + off) * w;
+    }
+    return 0;
+}
+
+struct Cube64 {
+    Grid64 G;
+    Vols64 V;
+    double k0;
+    int neq;
+};
+
+__device__ inline void rhs64(const Cube64& C, const double* y, double* f)
+{
+    double g[4];
+    lookup64(C.G, C.V, y, g);
+    f[0] = y[3];
+    f[1] = y[4];
+    f[2] = y[5];
+    f[3] = g[0];
+    f[4] = g[1];
+    f[5] = g[2];
+    if (C.neq == 7) {
+        const double q = g[3];
+        double r = 1.0 - q;
+        if (r < 0.0) r = 0.0;
+        const double nm1 = -q / (1.0 + sqrt(r));
+        const double sp = sqrt(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
+        f[6] = C.k0 * nm1 * sp;
+    }
+}
+
+__constant__ double kA[6][5] = {
+    {0, 0, 0, 0, 0},
+    {1.0 / 5, 0, 0, 0, 0},
+    {3.0 / 40, 9.0 / 40, 0, 0, 0},
+    {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0},
+    {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0},
+    {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656}};
+__constant__ double kB[6] = {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84};
+__constant__ double kE[7] = {-71.0 / 57600, 0, 71.0 / 16695, -71.0 / 1920, 17253.0 / 339200,
+                             -22.0 / 525, 1.0 / 40};
+
+template <int NEQ>
+__device__ inline double rms(const double* v)
+{
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) s += v[i] * v[i];
+    return sqrt(s) / sqrt((double)NEQ);
+}
+
+template <int NEQ>
+__device__ double initial_step64(const Cube64& C, const double* y0, const double* f0, double t_bound,
+                                 double rtol, double atol)
+{
+    double sc[NEQ], tmp[NEQ], y1[NEQ], f1[NEQ];
+    const double L = fabs(t_bound);
+    if (L == 0.0) return 0.0;
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) sc[i] = atol + fabs(y0[i]) * rtol;
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) tmp[i] = y0[i] / sc[i];
+    const double d0 = rms<NEQ>(tmp);
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) tmp[i] = f0[i] / sc[i];
+    const double d1 = rms<NEQ>(tmp);
+    double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
+    if (h0 > L) h0 = L;
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) y1[i] = y0[i] + h0 * f0[i];
+    rhs64(C, y1, f1);
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) tmp[i] = (f1[i] - f0[i]) / sc[i];
+    const double d2 = rms<NEQ>(tmp) / h0;
+    double h1;
+    if (d1 <= 1e-15 && d2 <= 1e-15) {
+        h1 = h0 * 1e-3;
+        if (h1 < 1e-6) h1 = 1e-6;
+    } else {
+        const double m = d1 > d2 ? d1 : d2;
+        h1 = pow(0.01 / m, 1.0 / 5.0);
+    }
+    double h = 100.0 * h0;
+    if (h1 < h) h = h1;
+    if (L < h) h = L;
+    return h;
+}
+
+template <int NEQ>
+__device__ int integrate64(const Cube64& C, double* y, double t_bound, double rtol, double atol,
+                           long long max_steps, int* nacc_out)
+{
+    double f[NEQ], K[7][NEQ], yn[NEQ], ys[NEQ];
+    for (int i = 0; i < NEQ; ++i)
+        if (!isfinite(y[i])) { *nacc_out = 0; return TT_RAY_NAN; }
+    rhs64(C, y, f);
+    long long nacc = 0, natt = 0;
+    double h_abs = initial_step64<NEQ>(C, y, f, t_bound, rtol, atol);
+    double t = 0.0;
+    int code = TT_RAY_OK;
+    if (t != t_bound) {
+        for (;;) {
+            const double min_step = 10.0 * fabs(nextafter(t, CUDART_INF) - t);
+            if (h_abs < min_step) h_abs = min_step;
+            bool rejected = false;
+            double t_new;
+            for (;;) {
+                if (h_abs < min_step) { code = TT_RAY_STEP_TOO_SMALL; break; }
+                if (natt >= max_steps) { code = TT_RAY_MAX_STEPS; break; }
+                ++natt;
+                double h = h_abs;
+                t_new = t + h;
+                if (t_new - t_bound > 0) t_new = t_bound;
+                h = t_new - t;
+                h_abs = fabs(h);
+#pragma unroll
+                for (int i = 0; i < NEQ; ++i) K[0][i] = f[i];
+#pragma unroll
+                for (int s = 1; s < 6; ++s) {
+#pragma unroll
+                    for (int i = 0; i < NEQ; ++i) {
+                        double acc = 0.0;
+#pragma unroll
+                        for (int j = 0; j < s; ++j) acc += K[j][i] * kA[s][j];
+                        ys[i] = y[i] + acc * h;
+                    }
+                    rhs64(C, ys, K[s]);
+                }
+#pragma unroll
+                for (int i = 0; i < NEQ; ++i) {
+                    double acc = 0.0;
+#pragma unroll
+                    for (int j = 0; j < 6; ++j) acc += K[j][i] * kB[j];
+                    yn[i] = y[i] + h * acc;
+                }
+                rhs64(C, yn, K[6]);
+                double es = 0.0;
+#pragma unroll
+                for (int i = 0; i < NEQ; ++i) {
+                    const double ay = fabs(y[i]), an = fabs(yn[i]);
+                    const double sc = atol + (ay > an ? ay : an) * rtol;
+                    double acc = 0.0;
+#pragma unroll
+                    for (int j = 0; j < 7; ++j) acc += K[j][i] * kE[j];
+                    const double e = acc * h / sc;
+                    es += e * e;
+                }
+                const double en = sqrt(es) / sqrt((double)NEQ);
+                if (en < 1.0) {
+                    double factor;
+                    if (en == 0.0) factor = 10.0;
+                    else {
+                        factor = 0.9 * pow(en, -0.2);
+                        if (!(factor < 10.0)) factor = 10.0;
+                    }
+                    if (rejected && !(factor < 1.0)) factor = 1.0;
+                    h_abs *= factor;
+                    break;
+                } else {
+                    double factor = 0.9 * pow(en, -0.2);
+                    if (!(factor > 0.2)) factor = 0.2;
+                    h_abs *= factor;
+                    rejected = true;
+                }
+            }
+            if (code != TT_RAY_OK) break;
+            ++nacc;
+            t = t_new;
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i) { y[i] = yn[i]; f[i] = K[6][i]; }
+            if (t - t_bound >= 0) break;
+        }
+    }
+    *nacc_out = (int)(nacc > 0x7fffffff ? 0x7fffffff : nacc);
+    return code;
+}
+
+// ray_at_exit, particle_tracker.py:333-380
+__device__ inline void ray_at_exit64(const double* y, int axis, double extent, double rf[4])
+{
+    const double x = y[0], yy = y[1], z = y[2], vx = y[3], vy = y[4], vz = y[5];
+    if (axis == 0) {
+        const double tbp = (x - extent) / vx;
+        rf[0] = yy - vy * tbp;
+        rf[2] = z - vz * tbp;
+        rf[1] = atan(vy / vx);
+        rf[3] = atan(vz / vx);
+    } else if (axis == 1) {
+        const double tbp = (yy - extent) / vy;
+        rf[0] = x - vx * tbp;
+        rf[2] = z - vz * tbp;
+        rf[1] = atan(vx / vy);
+        rf[3] = atan(vz / vy);
+    } else {
+        const double tbp = (z - extent) / vz;
+        rf[0] = x - vx * tbp;
+        rf[2] = yy - vy * tbp;
+        rf[1] = atan(vx / vz);
+        rf[3] = atan(vy / vz);
+    }
+}
+
+template <int NEQ>
+__global__ void __launch_bounds__(128, 1) trace64_kernel(Cube64 C, const double* __restrict__ s0, long long np,
+                                                      double t_end, int axis, double extent, double rtol,
+                                                      double atol, long long max_steps,
+                                                      double* __restrict__ sf, double* __restrict__ rf,
+                                                      double* __restrict__ phase, int* __restrict__ status,
+                                                      int* __restrict__ nsteps)
+{
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < np;
+         r += (long long)gridDim.x * blockDim.x) {
+        double y[NEQ];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) y[i] = s0[(size_t)i * np + r];
+        if (NEQ == 7) y[NEQ - 1] = 0.0;
+        int nacc = 0;
+        const int code = integrate64<NEQ>(C, y, t_end, rtol, atol, max_steps, &nacc);
+        if (sf) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) sf[(size_t)i * np + r] = y[i];
+        }
+        if (rf) {
+            double o[4];
+            ray_at_exit64(y, axis, extent, o);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) rf[(size_t)i * np + r] = o[i];
+        }
+        if (phase) phase[r] = NEQ == 7 ? y[NEQ - 1] : 0.0;
+        if (status) status[r] = code;
+        if (nsteps) nsteps[r] = nacc;
+    }
+}
+
+__global__ void dndr_kernel(Grid64 G, Vols64 V, const double* __restrict__ pts, long long npts,
+                            double* __restrict__ out)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npts;
+         i += (long long)gridDim.x * blockDim.x) {
+        double p[3] = {pts[i], pts[npts + i], pts[2 * npts + i]};
+        double o[4];
+        lookup64(G, V, p, o);
+        for (int k = 0; k < V.nvol; ++k) out[(size_t)k * npts + i] = o[k];
+    }
+}
+
+int make_grid(int nx, int ny, int nz, const double* x, const double* y, const double* z, Grid64* G)
+{
+    const double* cs[3] = {x, y, z};
+    const int n[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; ++a) {
+        G->g[a] = cs[a];
+        G->n[a] = n[a];
+    }
+    G->s0 = (size_t)ny * nz;
+    G->s1 = (size_t)nz;
+    return TT_OK;
+}
+
+int grid_size(long long n, int block)
+{
+    long long g = (n + block - 1) / block;
+    const long long cap = (long long)tt::sm_count() * 64;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+extern "C" int tt_dndr(const double* const* vols, int nvol, int nx, int ny, int nz, const double* x,
+                       const double* y, const double* z, const double* pts, int64_t npts, double* out,
+                       void* stream)
+{
+    if (!vols || nvol < 1 || nvol > 4) return tt::invalid("dndr: need 1..4 volumes");
+    if (nx < 2 || ny < 2 || nz < 2) return tt::invalid("dndr: every axis needs at least 2 points");
+    if (!x || !y || !z || (npts > 0 && (!pts || !out))) return tt::invalid("dndr: null pointer");
+    if (npts < 0) return tt::invalid("dndr: npts < 0");
+    if (npts == 0) return TT_OK;
+    Grid64 G;
+    TT_TRY(make_grid(nx, ny, nz, x, y, z, &G));
+    Vols64 V;
+    V.nvol = nvol;
+    for (int k = 0; k < 4; ++k) V.v[k] = k < nvol ? vols[k] : nullptr;
+    for (int k = 0; k < nvol; ++k)
+        if (!V.v[k]) return tt::invalid("dndr: null volume");
+    dndr_kernel<<<grid_size(npts, 256), 256, 0, tt::as_stream(stream)>>>(G, V, pts, npts, out);
+    return tt::launch_status("dndr kernel");
+}
+
+extern "C" int tt_trace_f64(const double* dndx, const double* dndy, const double* dndz, const double* ne_nc,
+                            int nx, int ny, int nz, const double* x, const double* y, const double* z,
+                            double omega, const double* s0, int64_t np, double t_end, int probing_axis,
+                            double extent, const tt_trace_opts* opts, double* sf, double* rf,
+                            double* phase, int32_t* status, int32_t* nsteps, void* stream)
+{
+    if (!opts) return tt::invalid("trace_f64: opts is null");
+    if (!dndx || !dndy || !dndz || !x || !y || !z) return tt::invalid("trace_f64: null pointer");
+    if (opts->with_phase && !ne_nc) return tt::invalid("trace_f64: phase needs ne_nc");
+    if (nx < 2 || ny < 2 || nz < 2) return tt::invalid("trace_f64: every axis needs at least 2 points");
+    if (probing_axis < 0 || probing_axis > 2) return tt::invalid("trace_f64: probing_axis must be 0, 1 or 2");
+    if (np < 0) return tt::invalid("trace_f64: np < 0");
+    if (!(opts->rtol > 0.0) || !(opts->atol >= 0.0)) return tt::invalid("trace_f64: need rtol > 0, atol >= 0");
+    if (!(t_end >= 0.0)) return tt::invalid("trace_f64: t_end must be >= 0");
+    if (np == 0) return TT_OK;
+    if (!s0) return tt::invalid("trace_f64: s0 is null");
+    Cube64 C;
+    TT_TRY(make_grid(nx, ny, nz, x, y, z, &C.G));
+    C.V.v[0] = dndx;
+    C.V.v[1] = dndy;
+    C.V.v[2] = dndz;
+    C.V.v[3] = ne_nc;
+    C.V.nvol = opts->with_phase ? 4 : 3;
+    C.k0 = omega / TT_C_LIGHT;
+    C.neq = opts->with_phase ? 7 : 6;
+    const long long maxs = opts->max_steps > 0 ? opts->max_steps : TT_DEFAULT_MAX_STEPS;
+    cudaStream_t s = tt::as_stream(stream);
+    const int block = 128;
+    if (opts->with_phase)
+        trace64_kernel<7><<<grid_size(np, block), block, 0, s>>>(C, s0, np, t_end, probing_axis, extent,
+                                                                 opts->rtol, opts->atol, maxs, sf, rf, phase,
+                                                                 status, nsteps);
+    else
+        trace64_kernel<6><<<grid_size(np, block), block, 0, s>>>(C, s0, np, t_end, probing_axis, extent,
+                                                                 opts->rtol, opts->atol, maxs, sf, rf, phase,
+                                                                 status, nsteps);
+    return tt::launch_status("trace_f64 kernel");
+}

@@ -72,7 +72,7 @@ def workload_config(a):
             "beam_sigma_m": a.sigma, "divergence_rad": a.div, "lwl_m": a.lwl,
             "detectors": ["shadowgraphy", "schlieren_knife_x0", "interferometry"], "detector_bins": [a.det, a.det],
             "detector_extent_mm": 12.0, "optics_f_mm": 100.0, "aperture_mm": 25.0,
-            "fp32_tol": {"rtol": 1e-6, "atol_cells": 1e-5, "atol_phase": 1e-5}, "seed": a.seed,
+            "fp32_tol": {"rtol": 1e-7, "atol_cells": 1e-5, "atol_phase": 1e-5}, "seed": a.seed,
             "l2": "inputs larger than L2 (density 0.5 GB, node volume 3.4 GB, rays 0.5 GB); no flush"}
 
 
@@ -218,7 +218,7 @@ def run_ours(a):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
-        core.trace_f32(vol, s0, t_end, ext, rtol=1e-6, atol=1e-5, atol_phase=1e-5, phase=True, ws=wsp, out=out)
+        core.trace_f32(vol, s0, t_end, ext, rtol=1e-7, atol=1e-5, atol_phase=1e-5, phase=True, ws=wsp, out=out)
         if record:
             e1.record()
             tr_ev.append((e0, e1))

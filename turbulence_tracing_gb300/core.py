@@ -184,7 +184,7 @@ def trace_f64(fields, s0, t_end, probing_axis, extent, rtol=1e-3, atol=1e-6, pha
     return out
 
 
-def trace_f32(vol, s0, t_end, extent, rtol=1e-6, atol=1e-5, atol_phase=1e-5, phase=False, max_steps=None,
+def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, phase=False, max_steps=None,
               want_sf=True, ws=None, out=None):
     """Persistent FP32 tracer over a Volume32.  s0: (6, Np) float64."""
     dev = require_cuda()

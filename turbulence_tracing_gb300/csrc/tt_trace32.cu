@@ -173,6 +173,7 @@ struct Ray {
     float sig, sigc;
     float ph, phc;
     float hctrl;
+    float hcap;    // one-shot cap on the next attempt after a face-crossing rejection
     int natt, nacc;
     int state;     // 0 = stepping, 1 = exited box, 2 = reached sigma_end, 3 = failed
     int code;
@@ -183,26 +184,101 @@ struct Ray {
     long long tbase;
 };
 
-constexpr float kFaceEps = 1e-3f;    // aim this far (cells) past an interior face
-constexpr float kBoxSnap = 1e-5f;    // closer than this to the box face, moving out: exited
+// Interior faces: a stage may use the current cell's polynomial up to kTolE
+// cells past a face, and a step may run at most kFacePath (path, in cells) past
+// the face it crosses; so a kink of the interpolant always sits within
+// kFacePath of a step end.  Box faces (where the field jumps to the fill value
+// 0): no extrapolation and at most kBoxPath of path past the face.
+constexpr float kTolE = 1e-3f;
+constexpr float kFacePath = 1e-3f;
+constexpr float kBoxPath = 1e-6f;
 
-__device__ __forceinline__ bool outside_cell(const Vol32& V, Ray& R)
+// Smallest h > 0 with v h + acc h^2 / 2 = d (d >= 0, moving from 0 toward d).
+__device__ __forceinline__ float first_hit(float v, float acc, float d)
 {
-    // normalise: P = ci + fr with fr in [0, 1); the upper box face belongs to the last cell
+    if (!(d > 0.f)) return 3.0e38f;
+    const float disc = fmaf(v, v, 2.f * acc * d);
+    if (disc < 0.f) return 3.0e38f;
+    const float den = v + sqrtf(disc);
+    return den > 0.f ? 2.f * d / den : 3.0e38f;
+}
+
+// Exact lookup (RegularGridInterpolator semantics, fill 0 outside) at cell
+// ci + floor(P), used when a stage leaves the current cell.  Scalars in,
+// float4 {H_a, H_b, H_c, q} out, so the caller's stage arrays stay in registers.
+__device__ __noinline__ float4 eval_exact(const float4* __restrict__ nodes, int n0, int n1, int n2, int st_b,
+                                          long long tile_f4, int c0, int c1, int c2, float p0, float p1, float p2)
+{
+    const int n[3] = {n0, n1, n2};
+    int c[3] = {c0, c1, c2};
+    const float P[3] = {p0, p1, p2};
+    float f[3];
+    bool out = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float fl = floorf(P[a]);
+        c[a] += (int)fl;
+        f[a] = P[a] - fl;
+        if (c[a] == n[a] - 1 && f[a] == 0.f) {
+            c[a] = n[a] - 2;
+            f[a] = 1.f;
+        }
+        out = out || c[a] < 0 || c[a] > n[a] - 2;
+    }
+    if (out) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const int ta = c[0] >> 2, tb = c[1] >> 2;
+    const uint32_t m = spread3((uint32_t)(ta & 7)) | (spread3((uint32_t)(tb & 7)) << 1);
+    const long long tbase = ((long long)((ta >> 3) * st_b + (tb >> 3)) * 64 + m) * tile_f4;
+    const long long base = tbase + (long long)(c[2] >> 3) * 200 + ((c[0] & 3) * 5 + (c[1] & 3)) * 8 + (c[2] & 7);
+    const int dc = ((c[2] & 7) == 7) ? 193 : 1;
+    const float4* p = nodes + base;
+    const float4 n000 = __ldg(p), n001 = __ldg(p + dc);
+    const float4 n010 = __ldg(p + 8), n011 = __ldg(p + 8 + dc);
+    const float4 n100 = __ldg(p + 40), n101 = __ldg(p + 40 + dc);
+    const float4 n110 = __ldg(p + 48), n111 = __ldg(p + 48 + dc);
+    const float fa = f[0], fb = f[1], fc = f[2];
+#define TT_LERP3(C)                                                                                  \
+    fmaf(fa, fmaf(fb, fmaf(fc, n111.C - n110.C, n110.C) - fmaf(fc, n101.C - n100.C, n100.C),         \
+                  fmaf(fc, n101.C - n100.C, n100.C)) -                                                \
+             fmaf(fb, fmaf(fc, n011.C - n010.C, n010.C) - fmaf(fc, n001.C - n000.C, n000.C),          \
+                  fmaf(fc, n001.C - n000.C, n000.C)),                                                 \
+         fmaf(fb, fmaf(fc, n011.C - n010.C, n010.C) - fmaf(fc, n001.C - n000.C, n000.C),              \
+              fmaf(fc, n001.C - n000.C, n000.C)))
+    const float4 r = make_float4(TT_LERP3(x), TT_LERP3(y), TT_LERP3(z), TT_LERP3(w));
+#undef TT_LERP3
+    return r;
+}
+
+// Normalise after an accepted step: P = ci + fr, fr in [0, 1), a ray within
+// kTolE of an interior face and moving through it is assigned to the cell it
+// enters; the upper box face belongs to the last cell.  Returns true when the
+// ray is outside the box.
+__device__ __forceinline__ bool renormalise(const Vol32& V, Ray& R)
+{
     bool out = false;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float fl = floorf(R.fr[a]);
-        if (fl != 0.0f) {
-            R.ci[a] += (int)fl;
-            R.fr[a] -= fl;
-            R.cell_dirty = true;
+        int c = R.ci[a] + (int)fl;
+        float f = R.fr[a] - fl;
+        if (c == V.n[a] - 1 && f == 0.f) {
+            c = V.n[a] - 2;
+            f = 1.f;
         }
-        if (R.ci[a] == V.n[a] - 1 && R.fr[a] == 0.0f) {
-            R.ci[a] = V.n[a] - 2;
-            R.fr[a] = 1.0f;
+        // pre-assign only when the face is within kFacePath of path ahead, so a
+        // slow (grazing) ray never runs far on the next cell's polynomial
+        const float vel = V.r[a] * R.u[a];
+        if (vel > 0.f && 1.f - f < fminf(kTolE, kFacePath * vel) && c < V.n[a] - 2) {
+            c += 1;
+            f -= 1.f;
+        } else if (vel < 0.f && f < fminf(kTolE, -kFacePath * vel) && c > 0) {
+            c -= 1;
+            f += 1.f;
         }
-        if (R.ci[a] < 0 || R.ci[a] > V.n[a] - 2) out = true;
+        if (c != R.ci[a]) R.cell_dirty = true;
+        R.ci[a] = c;
+        R.fr[a] = f;
+        out = out || c < 0 || c > V.n[a] - 2;
     }
     return out;
 }
@@ -234,6 +310,7 @@ __device__ __forceinline__ bool init_ray(const Vol32& V, const double* __restric
     R.sig = R.sigc = 0.f;
     R.ph = R.phc = 0.f;
     R.hctrl = 1.0f;
+    R.hcap = 3.0e38f;
     R.rejected = false;
     R.entered = false;
     R.code = TT_RAY_OK;
@@ -339,6 +416,34 @@ __device__ __forceinline__ void finish_ray(const Vol32& V, const Ray& R, const d
     if (nsteps) nsteps[r] = R.nacc;
 }
 
+// Right-hand side at stage position Ps (fractions in the current cell):
+// the current cell's polynomial while Ps stays within kTolE of it (never past
+// a box face), the exact lookup otherwise.
+__device__ __forceinline__ void stage_eval(const Vol32& V, const Ray& R, const float (*coef)[8], const float Ps[3],
+                                           float H[3], float& q)
+{
+    bool home = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float lo = R.ci[a] == 0 ? 0.f : -kTolE;
+        const float hi = R.ci[a] == V.n[a] - 2 ? 1.f : 1.f + kTolE;
+        home = home && Ps[a] >= lo && Ps[a] <= hi;
+    }
+    if (home) {
+        H[0] = tri(coef[0], Ps[0], Ps[1], Ps[2]);
+        H[1] = tri(coef[1], Ps[0], Ps[1], Ps[2]);
+        H[2] = tri(coef[2], Ps[0], Ps[1], Ps[2]);
+        q = V.with_phase ? tri(coef[3], Ps[0], Ps[1], Ps[2]) : 0.f;
+    } else {
+        const float4 r = eval_exact(V.nodes, V.n[0], V.n[1], V.n[2], V.st_b, V.tile_f4, R.ci[0], R.ci[1], R.ci[2],
+                                    Ps[0], Ps[1], Ps[2]);
+        H[0] = r.x;
+        H[1] = r.y;
+        H[2] = r.z;
+        q = r.w;
+    }
+}
+
 // One attempted step.  Returns with R updated.
 __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float (*coef)[8])
 {
@@ -352,28 +457,6 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
         load_cell(V, R.tbase, R.ci[0], R.ci[1], R.ci[2], coef);
         R.cell_dirty = false;
     }
-    // distance to the faces of the current cell along the ray
-    float hf = 3.0e38f;
-    bool at_box_face = false;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float vel = V.r[a] * R.u[a];
-        if (vel > 0.f) {
-            const bool boxf = R.ci[a] == V.n[a] - 2;
-            const float d = 1.0f - R.fr[a];
-            if (boxf && d < kBoxSnap) at_box_face = true;
-            hf = fminf(hf, (d + (boxf ? 0.f : kFaceEps)) / vel);
-        } else if (vel < 0.f) {
-            const bool boxf = R.ci[a] == 0;
-            const float d = R.fr[a];
-            if (boxf && d < kBoxSnap) at_box_face = true;
-            hf = fminf(hf, (d + (boxf ? 0.f : kFaceEps)) / (-vel));
-        }
-    }
-    if (at_box_face) {
-        R.state = 1;
-        return;
-    }
     const float rem = (float)(V.sig_end - ((double)R.sig + (double)R.sigc));
     if (!(rem > 0.f)) {
         R.state = 2;
@@ -384,19 +467,45 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
         R.state = 3;
         return;
     }
+    float Hs[7][3];
+    float q0;
+    stage_eval(V, R, coef, R.fr, Hs[0], q0);
+    // Predict the first face crossing of the cell from position, velocity and
+    // acceleration; aim the step end at it.  Leaving through a box face within
+    // kBoxPath: the ray has left (the field beyond is the fill value 0).
+    float hf = 3.0e38f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float vel = V.r[a] * R.u[a];
+        const float acc = V.r[a] * Hs[0][a];
+        const float hu = first_hit(vel, acc, 1.f - R.fr[a]);
+        const float hl = first_hit(-vel, -acc, R.fr[a]);
+        const bool box_up = R.ci[a] == V.n[a] - 2, box_lo = R.ci[a] == 0;
+        if ((box_up && vel > 0.f && (1.f - R.fr[a]) <= kBoxPath * vel) ||
+            (box_lo && vel < 0.f && R.fr[a] <= -kBoxPath * vel)) {
+            R.state = 1;
+            return;
+        }
+        hf = fminf(hf, fminf(hu, hl));
+    }
     ++R.natt;
     bool last = false;
-    float h = fminf(R.hctrl, hf);
+    float h = fminf(fminf(R.hctrl, R.hcap), hf);
+    R.hcap = 3.0e38f;
     if (h >= rem) {
         h = rem;
         last = true;
     }
-    // Stages: store H_k (3 comps); accumulate phase sums on the fly.
-    float Hs[7][3];
     float phb = 0.f, phe = 0.f;
     float Pn[3], un[3];
+    if (V.with_phase) {
+        const float sp = sqrtf(fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2])));
+        const float dph = V.kappa * nm1f(q0) * sp;
+        phb = T.b[0] * dph;
+        phe = T.e[0] * dph;
+    }
 #pragma unroll
-    for (int s = 0; s < 7; ++s) {
+    for (int s = 1; s < 7; ++s) {
         float Ps[3], us[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -409,11 +518,9 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
             us[c] = fmaf(h, sa, R.u[c]);
             Ps[c] = fmaf(h * V.r[c], fmaf(T.cs[s], R.u[c], h * saa), R.fr[c]);
         }
-        Hs[s][0] = tri(coef[0], Ps[0], Ps[1], Ps[2]);
-        Hs[s][1] = tri(coef[1], Ps[0], Ps[1], Ps[2]);
-        Hs[s][2] = tri(coef[2], Ps[0], Ps[1], Ps[2]);
+        float q;
+        stage_eval(V, R, coef, Ps, Hs[s], q);
         if (V.with_phase) {
-            const float q = tri(coef[3], Ps[0], Ps[1], Ps[2]);
             const float sp = sqrtf(fmaf(us[0], us[0], fmaf(us[1], us[1], us[2] * us[2])));
             const float dph = V.kappa * nm1f(q) * sp;
             if (s < 6) phb = fmaf(T.b[s], dph, phb);
@@ -457,42 +564,65 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
         neq = 7;
     }
     const float en = sqrtf(es / (float)neq);
-    if (en < 1.0f || !(en == en)) {
-        if (!(en == en)) {
-            R.code = TT_RAY_NAN;
-            R.state = 3;
-            return;
-        }
-        float factor = en == 0.f ? 10.f : fminf(10.f, 0.9f * __powf(en, -0.2f));
-        if (R.rejected) factor = fminf(1.f, factor);
-        R.rejected = false;
-        R.hctrl = h * factor;
-        ++R.nacc;
-        // commit
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            R.fr[c] = Pn[c];
-            R.u[c] = un[c];
-        }
-        {  // Kahan on sigma
-            const float y = __fsub_rn(h, R.sigc);
-            const float t = __fadd_rn(R.sig, y);
-            R.sigc = __fsub_rn(__fsub_rn(t, R.sig), y);
-            R.sig = t;
-        }
-        if (V.with_phase) neumaier(R.ph, R.phc, dphi);
-        const bool out = outside_cell(V, R);
-        if (out) R.state = 1;
-        else if (last) R.state = 2;
-    } else {
-        float factor = fmaxf(0.2f, 0.9f * __powf(en, -0.2f));
+    if (!(en == en)) {
+        R.code = TT_RAY_NAN;
+        R.state = 3;
+        return;
+    }
+    if (en >= 1.0f) {
+        const float factor = fmaxf(0.2f, 0.9f * __powf(en, -0.2f));
         R.hctrl = h * factor;
         R.rejected = true;
         if (R.hctrl < 1e-7f) {
             R.code = TT_RAY_STEP_TOO_SMALL;
             R.state = 3;
         }
+        return;
     }
+    // Where did the step cross a face?  If it ran too far past one, redo it
+    // ending at the crossing (estimated backwards from the end point).
+    float hre = 3.0e38f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float vend = V.r[a] * un[a];
+        float over = 0.f;  // path past the crossed face
+        bool box = false;
+        if (Pn[a] > 1.f && R.fr[a] <= 1.f) {
+            over = (Pn[a] - 1.f) / fmaxf(vend, 1e-6f);
+            box = R.ci[a] == V.n[a] - 2;
+        } else if (Pn[a] < 0.f && R.fr[a] >= 0.f) {
+            over = -Pn[a] / fmaxf(-vend, 1e-6f);
+            box = R.ci[a] == 0;
+        }
+        if (over > (box ? kBoxPath : kFacePath)) {
+            float hn = h - 1.01f * over;
+            if (!(hn > 0.1f * h)) hn = 0.5f * h;
+            hre = fminf(hre, hn);
+        }
+    }
+    if (hre < 3.0e38f) {
+        R.hcap = hre;  // controller state untouched: this was a geometric retry
+        return;
+    }
+    float factor = en == 0.f ? 10.f : fminf(10.f, 0.9f * __powf(en, -0.2f));
+    if (R.rejected) factor = fminf(1.f, factor);
+    R.rejected = false;
+    R.hctrl = h * factor;
+    ++R.nacc;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        R.fr[c] = Pn[c];
+        R.u[c] = un[c];
+    }
+    {  // Kahan on sigma
+        const float y = __fsub_rn(h, R.sigc);
+        const float t = __fadd_rn(R.sig, y);
+        R.sigc = __fsub_rn(__fsub_rn(t, R.sig), y);
+        R.sig = t;
+    }
+    if (V.with_phase) neumaier(R.ph, R.phc, dphi);
+    if (renormalise(V, R)) R.state = 1;
+    else if (last) R.state = 2;
 }
 
 __global__ void __launch_bounds__(128, 4)

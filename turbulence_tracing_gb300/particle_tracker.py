@@ -11,7 +11,7 @@ Additions (keyword-only, defaults keep the reference behaviour):
   solve(method='RK45', rtol=None, atol=None, precision='fp64', phase=False, max_steps=None)
     precision='fp64'  plain drop-in: per-ray RK45 with scipy's controller,
                       rtol/atol default to solve_ivp's 1e-3 / 1e-6;
-    precision='fp32'  persistent FP32 tracer (uniform grids), rtol default 1e-6
+    precision='fp32'  persistent FP32 tracer (uniform grids), rtol default 1e-7
                       on velocity/phase, atol default 1e-5 cells;
     phase=True        also integrates k0 * int (n - 1) ds into self.phase.
   set_up_interps()    (re)builds the device lookup state; calc_dndr calls it.
@@ -196,7 +196,7 @@ class ElectronCube:
         elif precision == "fp32":
             self._fields()
             out = core.trace_f32(self.volume32(), self.s0, t_end, extent,
-                                 rtol=1e-6 if rtol is None else rtol, atol=1e-5 if atol is None else atol,
+                                 rtol=1e-7 if rtol is None else rtol, atol=1e-5 if atol is None else atol,
                                  phase=phase, max_steps=max_steps)
         else:
             raise ValueError("precision must be 'fp64' or 'fp32'")

@@ -89,9 +89,10 @@ struct Vol32 {
     int axis[3];
     float kappa;
     double sig_end;
+    float sig_end_f;   // the same in FP32 for the step loop (no FP64 in the hot loop)
     double t_end;
     double extent;
-    float rtol, atol_cells, atol_phase;
+    float rtol, atol_cells, atol_phase, inv_rtol, inv_atol_cells;
     int with_phase;
     long long max_steps;
 };
@@ -154,7 +155,7 @@ __device__ inline float nm1f(float q)
 {
     float r = 1.0f - q;
     r = r > 0.0f ? r : 0.0f;
-    return -q / (1.0f + sqrtf(r));
+    return -__fdividef(q, 1.0f + r * rsqrtf(fmaxf(r, 1e-30f)));  // 2-ulp divide, ~1-ulp sqrt
 }
 
 // Neumaier summation s + x with running compensation c (no contraction).
@@ -199,8 +200,8 @@ __device__ __forceinline__ float first_hit(float v, float acc, float d)
     if (!(d > 0.f)) return 3.0e38f;
     const float disc = fmaf(v, v, 2.f * acc * d);
     if (disc < 0.f) return 3.0e38f;
-    const float den = v + sqrtf(disc);
-    return den > 0.f ? 2.f * d / den : 3.0e38f;
+    const float den = v + disc * rsqrtf(fmaxf(disc, 1e-30f));  // predictor only: approximate is fine
+    return den > 0.f ? __fdividef(2.f * d, den) : 3.0e38f;
 }
 
 // Exact lookup (RegularGridInterpolator semantics, fill 0 outside) at cell
@@ -457,7 +458,7 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
         load_cell(V, R.tbase, R.ci[0], R.ci[1], R.ci[2], coef);
         R.cell_dirty = false;
     }
-    const float rem = (float)(V.sig_end - ((double)R.sig + (double)R.sigc));
+    const float rem = (V.sig_end_f - R.sig) - R.sigc;
     if (!(rem > 0.f)) {
         R.state = 2;
         return;
@@ -499,7 +500,8 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
     float phb = 0.f, phe = 0.f;
     float Pn[3], un[3];
     if (V.with_phase) {
-        const float sp = sqrtf(fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2])));
+        const float u2 = fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2]));
+        const float sp = u2 * rsqrtf(u2);
         const float dph = V.kappa * nm1f(q0) * sp;
         phb = T.b[0] * dph;
         phe = T.e[0] * dph;
@@ -521,7 +523,8 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
         float q;
         stage_eval(V, R, coef, Ps, Hs[s], q);
         if (V.with_phase) {
-            const float sp = sqrtf(fmaf(us[0], us[0], fmaf(us[1], us[1], us[2] * us[2])));
+            const float u2 = fmaf(us[0], us[0], fmaf(us[1], us[1], us[2] * us[2]));
+            const float sp = u2 * rsqrtf(u2);
             const float dph = V.kappa * nm1f(q) * sp;
             if (s < 6) phb = fmaf(T.b[s], dph, phb);
             phe = fmaf(T.e[s], dph, phe);
@@ -536,9 +539,9 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
     }
     // error estimate; velocity scale is rtol times the speed (|u| ~ 1), so the
     // velocity tolerance is an angle
-    const float sp0 = sqrtf(fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2])));
-    const float sp1 = sqrtf(fmaf(un[0], un[0], fmaf(un[1], un[1], un[2] * un[2])));
-    const float scu = V.rtol * fmaxf(sp0, sp1) + 1e-30f;
+    const float q0u = fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2]));
+    const float q1u = fmaf(un[0], un[0], fmaf(un[1], un[1], un[2] * un[2]));
+    const float inv_scu = rsqrtf(fmaxf(q0u, q1u)) * V.inv_rtol;  // 1 / (rtol |u|)
     float es = 0.f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -549,8 +552,8 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
         for (int k = 0; k < 6; ++k) ep = fmaf(T.ea[k], Hs[k][c], ep);
         eu *= h;
         ep *= h * h * V.r[c];
-        const float x1 = eu / scu;
-        const float x2 = ep / V.atol_cells;
+        const float x1 = eu * inv_scu;
+        const float x2 = ep * V.inv_atol_cells;
         es = fmaf(x1, x1, fmaf(x2, x2, es));
     }
     int neq = 6;
@@ -559,11 +562,11 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
         dphi = h * phb;
         const float phn = R.ph + dphi;
         const float scp = V.atol_phase + V.rtol * fmaxf(fabsf(R.ph), fabsf(phn));
-        const float x = h * phe / scp;
+        const float x = __fdividef(h * phe, scp);
         es = fmaf(x, x, es);
         neq = 7;
     }
-    const float en = sqrtf(es / (float)neq);
+    const float en = sqrtf(es * (neq == 7 ? (1.f / 7.f) : (1.f / 6.f)));
     if (!(en == en)) {
         R.code = TT_RAY_NAN;
         R.state = 3;
@@ -588,10 +591,10 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
         float over = 0.f;  // path past the crossed face
         bool box = false;
         if (Pn[a] > 1.f && R.fr[a] <= 1.f) {
-            over = (Pn[a] - 1.f) / fmaxf(vend, 1e-6f);
+            over = __fdividef(Pn[a] - 1.f, fmaxf(vend, 1e-6f));
             box = R.ci[a] == V.n[a] - 2;
         } else if (Pn[a] < 0.f && R.fr[a] >= 0.f) {
-            over = -Pn[a] / fmaxf(-vend, 1e-6f);
+            over = __fdividef(-Pn[a], fmaxf(-vend, 1e-6f));
             box = R.ci[a] == 0;
         }
         if (over > (box ? kBoxPath : kFacePath)) {
@@ -625,7 +628,10 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
     else if (last) R.state = 2;
 }
 
-__global__ void __launch_bounds__(128, 4)
+#ifndef TT_TRACE32_MIN_BLOCKS
+#define TT_TRACE32_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(128, TT_TRACE32_MIN_BLOCKS)
 trace32_kernel(Vol32 V, Tab T, const double* __restrict__ s0, long long np,
                const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
                double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
@@ -812,10 +818,13 @@ extern "C" int tt_trace_f32(const tt_volume* vol, const double* s0, int64_t np, 
     V.tile_f4 = (long long)vol->bricks_c * 200;
     V.kappa = (float)(vol->omega / TT_C_LIGHT * vol->spacing[2]);
     V.sig_end = t_end * TT_C_LIGHT / vol->spacing[2];
+    V.sig_end_f = (float)V.sig_end;
     V.t_end = t_end;
     V.extent = extent;
     V.rtol = (float)opts->rtol;
     V.atol_cells = (float)opts->atol;
+    V.inv_rtol = (float)(1.0 / opts->rtol);
+    V.inv_atol_cells = (float)(1.0 / opts->atol);
     V.atol_phase = (float)(opts->with_phase ? opts->atol_phase : 1.0);
     V.with_phase = opts->with_phase ? 1 : 0;
     V.max_steps = opts->max_steps > 0 ? opts->max_steps : TT_DEFAULT_MAX_STEPS;

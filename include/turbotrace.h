@@ -69,6 +69,23 @@ int tt_calc_dndr(const void* ne, int ne_dtype, int nx, int ny, int nz,
                  double* omega_out /* host, may be NULL */,
                  void* workspace, size_t workspace_bytes, void* stream);
 
+/* tt_calc_dndr_noalloc -- no counterpart in the reference.  The same results
+ * as tt_calc_dndr for callers that cannot allocate device memory (a host
+ * whose allocator owns all device buffers, or work enqueued while a stream is
+ * being captured into a CUDA graph, where cudaMalloc is not allowed).  It
+ * allocates nothing: its scratch is a fixed 590 KB device array inside the
+ * library, present on every GPU that loads it until the process exits, so
+ * every axis is limited to 8192 nodes (TT_ERR_TOO_LARGE beyond).  The first
+ * call on a device looks up that array's device address (no allocation);
+ * make that first call before any stream capture.  All calls share the
+ * array: calls whose work overlaps on the GPU (other streams, other threads)
+ * race and must be serialised by the caller. */
+int tt_calc_dndr_noalloc(const void* ne, int ne_dtype, int nx, int ny, int nz,
+                         const double* x, const double* y, const double* z,
+                         double lwl, double ne_max,
+                         double* ne_nc, double* dndx, double* dndy, double* dndz,
+                         double* omega_out /* host, may be NULL */, void* stream);
+
 /* dndr -- replaces ElectronCube.dndr, particle_tracker.py:243-256 (the
  * RegularGridInterpolator lookups built at :239-241): trilinear, fill 0
  * outside the grid, NaN in -> NaN out.  pts: (3, npts) SoA; out: (nvol, npts)

@@ -68,6 +68,9 @@ SIGNATURES = {
     "tt_calc_dndr": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
                              ctypes.c_double, ctypes.c_double, c_void_p, c_void_p, c_void_p, c_void_p,
                              c_double_p, c_void_p, c_size, c_void_p]),
+    "tt_calc_dndr_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                     ctypes.c_double, ctypes.c_double, c_void_p, c_void_p, c_void_p, c_void_p,
+                                     c_double_p, c_void_p]),
     "tt_dndr": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
                         c_void_p, c_i64, c_void_p, c_void_p]),
     "tt_volume_plan": (c_int, [c_int, c_int, c_int, c_double_p, c_double_p, c_double_p, c_int,

@@ -12,6 +12,8 @@
 // FP32 reads ~4-8 B and writes 16 B per stored node (apron nodes included).
 #include <math.h>
 
+#include <mutex>
+
 #include "tt_common.cuh"
 
 namespace {
@@ -175,6 +177,93 @@ extern "C" int tt_calc_dndr(const void* ne, int ne_dtype, int nx, int ny, int nz
     TT_TRY(tt::launch_status("calc_dndr ne_nc kernel"));
     dndr_grad_kernel<<<grid_for(nv, 256), 256, 0, s>>>(ne_nc, nx, ny, nz, tx, ty, tz, k, dndx, dndy, dndz);
     return tt::launch_status("calc_dndr gradient kernel");
+}
+
+// ===========================================================================
+// calc_dndr without any allocation.
+//
+// For callers that cannot allocate device memory for the workspace: a host
+// application whose allocator owns every device buffer and forbids other
+// allocations, or code that enqueues work while its stream is being captured
+// into a CUDA graph (cudaMalloc is not allowed during capture).  The
+// numpy.gradient coefficient tables then live in the fixed array below,
+// which every GPU that loads this library keeps until the process exits.
+// ===========================================================================
+namespace {
+
+constexpr int kNoAllocMaxAxis = 8192;  // nodes per axis the fixed tables can hold
+constexpr size_t kNoAllocDoubles = 3 * (4 + 3 * (size_t)kNoAllocMaxAxis);  // 590 KB
+
+std::mutex g_noalloc_mutex;
+double* g_noalloc_tables[64] = {nullptr};  // device address of g_calc_dndr_tables, per device
+
+}  // namespace
+
+static __device__ __align__(256) double g_calc_dndr_tables[kNoAllocDoubles];
+
+namespace {
+
+// Device address of the fixed tables on the current device, looked up once per
+// device (the host-side name of a __device__ array is not a device address).
+int noalloc_tables(double** out)
+{
+    int dev = 0;
+    TT_TRY(tt::cuda_status(cudaGetDevice(&dev), "calc_dndr_noalloc: cudaGetDevice"));
+    if (dev < 0 || dev >= 64) return tt::invalid("calc_dndr_noalloc: device index above 63");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_tables[dev]) {
+        void* p = nullptr;
+        TT_TRY(tt::cuda_status(cudaGetSymbolAddress(&p, g_calc_dndr_tables),
+                               "calc_dndr_noalloc: cudaGetSymbolAddress"));
+        g_noalloc_tables[dev] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_tables[dev];
+    return TT_OK;
+}
+
+}  // namespace
+
+extern "C" int tt_calc_dndr_noalloc(const void* ne, int ne_dtype, int nx, int ny, int nz, const double* x,
+                                    const double* y, const double* z, double lwl, double ne_max, double* ne_nc,
+                                    double* dndx, double* dndy, double* dndz, double* omega_out, void* stream)
+{
+    if (nx < 2 || ny < 2 || nz < 2)
+        return tt::invalid("calc_dndr_noalloc: every axis needs at least 2 points (numpy.gradient edge_order=1)");
+    if (nx > kNoAllocMaxAxis || ny > kNoAllocMaxAxis || nz > kNoAllocMaxAxis) {
+        tt::set_detail("calc_dndr_noalloc: at most %d nodes per axis (got %d x %d x %d); use tt_calc_dndr "
+                       "with a workspace for larger grids", kNoAllocMaxAxis, nx, ny, nz);
+        return TT_ERR_TOO_LARGE;
+    }
+    if (!ne || !x || !y || !z || !ne_nc || !dndx || !dndy || !dndz)
+        return tt::invalid("calc_dndr_noalloc: null pointer");
+    if (ne_dtype != TT_F32 && ne_dtype != TT_F64)
+        return tt::invalid("calc_dndr_noalloc: ne_dtype must be TT_F32 or TT_F64");
+    if (!(lwl > 0.0)) return tt::invalid("calc_dndr_noalloc: lwl must be > 0");
+    double* tx = nullptr;
+    TT_TRY(noalloc_tables(&tx));
+    const double omega = (2.0 * M_PI) * (TT_C_LIGHT / lwl);
+    const double nc = 3.14207787e-4 * (omega * omega);
+    const double k = -0.5 * (TT_C_LIGHT * TT_C_LIGHT);
+    if (omega_out) *omega_out = omega;
+    cudaStream_t s = tt::as_stream(stream);
+    // every table entry the gradient kernel reads is rewritten here first, so
+    // nothing needs clearing between calls
+    double* ty = tx + axis_table_doubles(nx);
+    double* tz = ty + axis_table_doubles(ny);
+    grad_coef_kernel<<<1, 256, 0, s>>>(x, nx, tx);
+    grad_coef_kernel<<<1, 256, 0, s>>>(y, ny, ty);
+    grad_coef_kernel<<<1, 256, 0, s>>>(z, nz, tz);
+    TT_TRY(tt::launch_status("calc_dndr_noalloc coefficient kernel"));
+    const size_t nv = (size_t)nx * ny * nz;
+    if (ne_dtype == TT_F64)
+        ne_nc_kernel<double><<<grid_for(nv, 256), 256, 0, s>>>(static_cast<const double*>(ne), nv, nc,
+                                                                ne_max, ne_nc);
+    else
+        ne_nc_kernel<float><<<grid_for(nv, 256), 256, 0, s>>>(static_cast<const float*>(ne), nv, nc,
+                                                               ne_max, ne_nc);
+    TT_TRY(tt::launch_status("calc_dndr_noalloc ne_nc kernel"));
+    dndr_grad_kernel<<<grid_for(nv, 256), 256, 0, s>>>(ne_nc, nx, ny, nz, tx, ty, tz, k, dndx, dndy, dndz);
+    return tt::launch_status("calc_dndr_noalloc gradient kernel");
 }
 
 // ===========================================================================

@@ -56,9 +56,9 @@ def parse():
     ap.add_argument("--det", type=int, default=1024)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--fp64-rays", type=int, default=20000)
-    ap.add_argument("--check-rays", type=int, default=4000)
-    ap.add_argument("--cpu-rays", type=int, default=3000)
-    ap.add_argument("--ref-rays", type=int, default=1500)
+    ap.add_argument("--check-rays", type=int, default=2000)
+    ap.add_argument("--cpu-rays", type=int, default=30000)
+    ap.add_argument("--ref-rays", type=int, default=8000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
@@ -289,41 +289,57 @@ def run_ours(a):
 
 
 def fp64_compare(a, core, ne, x, s0_host, t_end, ext, out32, rays_per_s32):
-    """Plain FP64 drop-in on a ray subset: (1) at the tolerance that meets the
-    accuracy bar, timed; (2) at rtol 1e-10 as the FP64 reference for the FP32 error."""
+    """Plain FP64 drop-in on a ray subset at several tolerances, each timed and
+    checked against the FP64 drop-in at rtol 1e-11 / atol 1e-13 (the reference
+    for the accuracy bars); the FP32 tracer's errors against the same reference.
+    The equal-accuracy speed-up uses the loosest FP64 tolerance that meets the bars."""
     import torch
 
     fields = core.calc_dndr(ne, x, x, x, lwl=a.lwl)
     m = min(a.fp64_rays, s0_host.shape[1])
-    sub = torch.as_tensor(np.ascontiguousarray(s0_host[:, :m]), device="cuda")
-    core.trace_f64(fields, sub[:, :min(m, 256)], t_end, 2, ext, rtol=1e-8, atol=1e-11, phase=True)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    o64 = core.trace_f64(fields, sub, t_end, 2, ext, rtol=1e-8, atol=1e-11, phase=True)
-    e1.record()
-    torch.cuda.synchronize()
-    sec = e0.elapsed_time(e1) / 1e3
-    steps64 = int(o64["nsteps"].sum().item())
     c = min(a.check_rays, m)
-    ref = core.trace_f64(fields, sub[:, :c], t_end, 2, ext, rtol=1e-10, atol=1e-12, phase=True)
+    sub = torch.as_tensor(np.ascontiguousarray(s0_host[:, :m]), device="cuda")
+    ref = core.trace_f64(fields, sub[:, :c], t_end, 2, ext, rtol=1e-11, atol=1e-13, phase=True)
     torch.cuda.synchronize()
     rf_ref = ref["rf"].cpu().numpy()
     ph_ref = ref["phase"].cpu().numpy()
-    acc = {}
-    for name, rf, ph in (("fp32", out32["rf"][:, :c].cpu().numpy(), out32["phase"][:c].cpu().numpy()),
-                         ("fp64_plain_rtol1e-8", o64["rf"][:, :c].cpu().numpy(), o64["phase"][:c].cpu().numpy())):
-        acc[name] = {"pos_over_L": float(np.abs(rf[0::2] - rf_ref[0::2]).max() / a.L),
-                     "angle_rad": float(np.abs(rf[1::2] - rf_ref[1::2]).max()),
-                     "phase_rad": float(np.abs(ph - ph_ref).max())}
-    acc["reference"] = "FP64 drop-in at rtol 1e-10, atol 1e-12 on %d rays (matches the CPU oracle to ~1e-10)" % c
-    acc["bars"] = {"pos_over_L": 1e-6, "angle_rad": 1e-6, "phase_rad": 1e-3}
+    bars = {"pos_over_L": 1e-6, "angle_rad": 1e-6, "phase_rad": 1e-3}
+
+    def err(rf, ph):
+        return {"pos_over_L": float(np.abs(rf[0::2] - rf_ref[0::2]).max() / a.L),
+                "angle_rad": float(np.abs(rf[1::2] - rf_ref[1::2]).max()),
+                "phase_rad": float(np.abs(ph - ph_ref).max())}
+
+    def meets(e):
+        return all(e[k] <= bars[k] for k in bars)
+
+    acc = {"fp32": err(out32["rf"][:, :c].cpu().numpy(), out32["phase"][:c].cpu().numpy())}
+    acc["fp32"]["meets_bars"] = meets(acc["fp32"])
+    runs = []
+    for rtol, atol in ((1e-8, 1e-11), (1e-9, 1e-12), (1e-10, 1e-13)):
+        core.trace_f64(fields, sub[:, :256], t_end, 2, ext, rtol=rtol, atol=atol, phase=True)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        o64 = core.trace_f64(fields, sub, t_end, 2, ext, rtol=rtol, atol=atol, phase=True)
+        e1.record()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        steps = int(o64["nsteps"].sum().item())
+        e = err(o64["rf"][:, :c].cpu().numpy(), o64["phase"][:c].cpu().numpy())
+        e["meets_bars"] = meets(e)
+        runs.append({"rtol": rtol, "atol": atol, "rays": m, "seconds": sec, "ray_steps": steps,
+                     "ray_steps_per_s": steps / sec, "rays_per_s": m / sec, "error": e})
+        if e["meets_bars"]:
+            break
+    acc["reference"] = "FP64 drop-in at rtol 1e-11, atol 1e-13 on %d rays (the tests tie it to the CPU oracle)" % c
+    acc["bars"] = bars
     del fields
     torch.cuda.empty_cache()
-    f64 = {"rays": m, "rtol": 1e-8, "atol": 1e-11, "seconds": sec, "ray_steps": steps64,
-           "ray_steps_per_s": steps64 / sec, "rays_per_s": m / sec,
-           "fp32_speedup_equal_accuracy_rays_per_s": rays_per_s32 / (m / sec)}
+    at_bar = next((r for r in runs if r["error"]["meets_bars"]), runs[-1])
+    f64 = {"runs": runs, "at_bar": {k: at_bar[k] for k in ("rtol", "atol", "rays_per_s", "ray_steps_per_s")},
+           "fp32_speedup_equal_accuracy_rays_per_s": rays_per_s32 / at_bar["rays_per_s"]}
     return f64, acc
 
 

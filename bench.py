@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--fp64-rays", type=int, default=20000)
     ap.add_argument("--check-rays", type=int, default=2000)
-    ap.add_argument("--cpu-rays", type=int, default=30000)
+    ap.add_argument("--cpu-rays", type=int, default=8000)
     ap.add_argument("--ref-rays", type=int, default=8000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -202,5 +202,5 @@ def test_f32_null_field_is_straight(cuda):
     T = 2 * x.max() / s0[5]
     want = np.stack([s0[0] + s0[3] * T, np.arctan(s0[3] / s0[5]), s0[1] + s0[4] * T, np.arctan(s0[4] / s0[5])])
     e = errors(rf, want, 2 * x.max())
-    assert e["pos"] < 1e-7 and e["ang"] < 1e-9, e  # FP32 cell fractions: ~1e-7 cell per step
+    assert e["pos"] < 1e-7 and e["ang"] < 1e-8, e  # FP32 state: ~1e-7 relative in angle, ~1e-7 cell per step
     assert np.abs(out["phase"].cpu().numpy()).max() == 0.0

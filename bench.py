@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=64)
     ap.add_argument("--json-out", default="")
     return ap.parse_args()
 
@@ -281,6 +283,10 @@ def run_ours(a):
         res["fp64_dropin"], res["accuracy"] = fp64_compare(a, core, ne, x, s0_host, t_end, ext, out, rays_per_s / ws)
     if not a.no_e2e:
         res["e2e"] = e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist)
+    if rank == 0 and not a.no_batched:
+        del out, wsp, vol
+        torch.cuda.empty_cache()
+        res["batched"] = batched_run(a)
     if rank == 0 and not a.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(a, ne, x)
     if dist:
@@ -341,6 +347,54 @@ def fp64_compare(a, core, ne, x, s0_host, t_end, ext, out32, rays_per_s32):
     f64 = {"runs": runs, "at_bar": {k: at_bar[k] for k in ("rtol", "atol", "rays_per_s", "ray_steps_per_s")},
            "fp32_speedup_equal_accuracy_rays_per_s": rays_per_s32 / at_bar["rays_per_s"]}
     return f64, acc
+
+
+def batched_run(a):
+    """The batched ensemble: a.batch_instances realisations drawn as the batched
+    workload (grid 128/192/256/384^3, exponent -5/3/-3/-11/3, delta in
+    [0.05, 0.3], background 1e23..1e25 m^-3, 1e5..4e6 rays log-uniform,
+    sigma 0.25 L, 0.05 mrad, L = 2 mm, 512^2 shadowgram each), traced in one
+    persistent launch replayed from a CUDA graph, against the same work as one
+    launch per instance without a graph."""
+    import torch
+
+    from turbulence_tracing_gb300 import ensemble
+
+    inst = ensemble.draw_instances(a.batch_instances, seed=a.seed)
+    E = ensemble.Ensemble(inst, L=2e-3, det=512, phase=False, tune=True).setup()
+    E.capture()
+    for _ in range(2):
+        E.replay()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = 3
+    e0.record()
+    for _ in range(reps):
+        E.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    steps = E.ray_steps()
+    bad = int((E.out["status"] != 0).sum().item())
+    E.run_unbatched()
+    torch.cuda.synchronize()
+    e0.record()
+    E.run_unbatched()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_unb = e0.elapsed_time(e1)
+    sizes = {}
+    for p in inst:
+        sizes[p["n"]] = sizes.get(p["n"], 0) + 1
+    return {"instances": len(inst), "rays": E.ntot, "grid_counts": {str(k): v for k, v in sorted(sizes.items())},
+            "ray_steps_per_step": steps, "ms_per_step": ms, "ray_steps_per_s": steps / (ms / 1e3),
+            "rays_per_s": E.ntot / (ms / 1e3), "non_ok_rays": bad,
+            "unbatched_ms_per_step": ms_unb, "speedup_vs_one_launch_per_instance": ms_unb / ms,
+            "block_size": E.block, "block_ms": {str(k): v for k, v in getattr(E, "block_ms", {}).items()},
+            "autotuned_per_grid": {str(k): {"block": v["block"], "brick_depth": v["brick_depth"]}
+                                   for k, v in E.tuned.items()},
+            "pipeline": "CUDA graph: 64 volume builds + bucketing + one batched trace launch + 64 shadowgrams"}
 
 
 def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):

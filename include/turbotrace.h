@@ -100,15 +100,16 @@ int tt_dndr(const double* const* vols, int nvol, int nx, int ny, int nz,
  * i.e. the deflection per cell length of the probing axis.  Layout: the
  * probing axis c is fastest; the transverse axes a, b are cut into 4x4-cell
  * tiles stored with a one-node apron (5x5 node columns), each tile column cut
- * into bricks of 8 nodes along c; tiles are ordered by Morton code inside 8x8
- * super-tiles, super-tiles row-major.  Requires uniformly spaced coordinates. */
+ * into bricks of brick_depth nodes along c; tiles are ordered by Morton code
+ * inside 8x8 super-tiles, super-tiles row-major.  Requires uniformly spaced
+ * coordinates. */
 typedef struct tt_volume {
     int32_t n[3];          /* nodes along a, b, c */
     int32_t axis[3];       /* physical axis (0=x, 1=y, 2=z) of a, b, c */
     int32_t tiles[2];      /* 4-cell tiles along a, b */
     int32_t supertiles[2]; /* 8x8-tile super-tiles along a, b */
-    int32_t bricks_c;      /* 8-node bricks along c */
-    int32_t reserved;
+    int32_t bricks_c;      /* bricks along c */
+    int32_t brick_depth;   /* nodes per brick along c (power of two, 4..32; tt_volume_plan sets 8) */
     double origin[3];      /* coordinate (m) of node 0 along a, b, c */
     double spacing[3];     /* node spacing (m) along a, b, c */
     double omega;          /* laser angular frequency (rad/s) */
@@ -123,6 +124,9 @@ typedef struct tt_volume {
 int tt_volume_plan(int nx, int ny, int nz, const double* x_host, const double* y_host,
                    const double* z_host, int probing_axis, double lwl, double ne_max,
                    tt_volume* vol);
+/* Change the brick depth (power of two, 4..32) of a planned volume; updates
+ * bricks_c and n_float4.  Call before sizing and building the node buffer. */
+int tt_volume_set_brick_depth(tt_volume* vol, int brick_depth);
 /* Write the node buffer from a density (nx,ny,nz) of ne_dtype. */
 int tt_volume_build(const tt_volume* vol, const void* ne, int ne_dtype, void* stream);
 
@@ -141,7 +145,7 @@ typedef struct tt_trace_opts {
     double atol_phase;  /* FP32 only: absolute phase tolerance (rad) */
     int64_t max_steps;  /* per-ray cap on attempted steps; 0 = TT_DEFAULT_MAX_STEPS */
     int32_t with_phase; /* integrate the phase as an extra state */
-    int32_t reserved;
+    int32_t block_size; /* FP32 tracer: threads per block, 64, 128 or 256 (0 = 128) */
 } tt_trace_opts;
 
 /* Plain FP64 drop-in: scipy RK45 controller per ray (safety 0.9, factors
@@ -164,6 +168,23 @@ int tt_trace_f32(const tt_volume* vol, const double* s0, int64_t np, double t_en
                  const tt_trace_opts* opts, double* sf, double* rf, double* phase,
                  int32_t* status, int32_t* nsteps, void* workspace, size_t workspace_bytes,
                  void* stream);
+
+/* Batched form: ninst field realisations (each its own tt_volume, grid size,
+ * t_end and exit plane) traced in ONE persistent launch.  Arrays are
+ * instance-blocked: instance i owns rays [ray_offsets[i], ray_offsets[i+1]),
+ * n_i of them, and its s0 is a (6, n_i) block starting at element
+ * 6 * ray_offsets[i] of s0 (sf likewise, rf a (4, n_i) block at
+ * 4 * ray_offsets[i], phase/status/nsteps at ray_offsets[i]), so each
+ * instance's results are ordinary arrays for tt_detect.  Rays are bucketed by
+ * (instance, entry tile) and pulled from one work queue, each lane carrying
+ * its ray's instance.  vols, ray_offsets, t_end and extent are host arrays; at
+ * most TT_MAX_INSTANCES instances. */
+#define TT_MAX_INSTANCES 128
+size_t tt_trace_f32_batched_workspace_bytes(const tt_volume* vols, int ninst, int64_t ntot);
+int tt_trace_f32_batched(const tt_volume* vols, int ninst, const int64_t* ray_offsets, const double* t_end,
+                         const double* extent, const double* s0, const tt_trace_opts* opts,
+                         double* sf, double* rf, double* phase, int32_t* status, int32_t* nsteps,
+                         void* workspace, size_t workspace_bytes, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* K3  detectors -- replaces Rays.__init__/solve/histogram and the filters of

@@ -1,0 +1,105 @@
+"""Batched ensemble (one persistent launch over many realisations, CUDA-graph
+pipeline, autotuned block and brick shapes) against the single-volume tracer,
+which the other tests tie to the oracle.  A ray's arithmetic does not depend
+on which launch, block size or brick depth carries it, so the comparisons
+are exact."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import restated as R
+from tests.cases import LWL, errors, oracle_trace
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_ensemble(**kw):
+    from turbulence_tracing_gb300 import ensemble
+
+    inst = ensemble.draw_instances(n_inst=6, seed=3, sizes=(24, 32, 40), rays=(200, 3000))
+    inst[2]["nrays"] = 0  # an instance with no rays
+    return ensemble.Ensemble(inst, L=1e-3, det=64, phase=True, **kw).setup()
+
+
+def test_batched_equals_single_launches(cuda):
+    from turbulence_tracing_gb300 import core
+
+    E = _small_ensemble(tune=False)
+    torch.cuda.synchronize()
+    rf_b = E.out["rf"].clone()
+    ph_b = E.out["phase"].clone()
+    ns_b = E.out["nsteps"].clone()
+    singles = E.run_unbatched()
+    torch.cuda.synchronize()
+    for i, o in enumerate(singles):
+        b, e = E.offsets[i], E.offsets[i + 1]
+        assert torch.equal(core.ray_block(rf_b, 4, E.offsets, i), o["rf"])
+        assert torch.equal(ph_b[b:e], o["phase"][: e - b])
+        assert torch.equal(ns_b[b:e], o["nsteps"][: e - b])
+    assert (E.out["status"] == 0).all()
+
+
+def test_batched_instance_against_oracle(cuda):
+    from turbulence_tracing_gb300 import core
+
+    E = _small_ensemble(tune=False)
+    i = int(np.argmax(np.diff(E.offsets)))
+    x = E.coords[i]
+    ne = E.fields[i].double().cpu().numpy()
+    s0 = core.ray_block(E.s0, 6, E.offsets, i)[:, :300].cpu().numpy()
+    ref = oracle_trace(ne, x, s0)
+    rf = core.ray_block(E.out["rf"], 4, E.offsets, i)[:, :300].cpu().numpy()
+    b = E.offsets[i]
+    ph = E.out["phase"][b:b + 300].cpu().numpy()
+    e = errors(rf, ref["rf"], 2 * x.max(), ph, ref["phase"])
+    assert e["pos"] <= 1e-6 and e["ang"] <= 1e-6 and e["phase"] <= 1e-3, e
+
+
+def test_brick_depth_and_block_size_do_not_change_results(cuda):
+    from turbulence_tracing_gb300 import core
+
+    ne, x = R.workload_density(36, 1e-3, -5 / 3, 0.2, 5e24, 4)
+    s0 = R.gaussian_beam(2000, 0.25e-3, 1e-3, x.max(), np.random.default_rng(2))
+    t_end = R.t_end(x.max())
+    ref = None
+    for bd in (4, 8, 16, 32):
+        vol = core.build_volume(ne, x, x, x, 2, lwl=LWL, brick_depth=bd)
+        for block in (64, 128, 256):
+            o = core.trace_f32(vol, s0, t_end, x.max(), phase=True, block_size=block)
+            got = (o["rf"].cpu(), o["phase"].cpu(), o["nsteps"].cpu())
+            if ref is None:
+                ref = got
+            else:
+                assert all(torch.equal(a, b) for a, b in zip(got, ref)), (bd, block)
+
+
+def test_graph_replay_matches_eager(cuda):
+    E = _small_ensemble(tune=False)
+    torch.cuda.synchronize()
+    H_eager = E.H.clone()
+    rf_eager = E.out["rf"].clone()
+    E.out["rf"].zero_()
+    E.H.zero_()
+    E.capture()
+    E.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(E.out["rf"], rf_eager)
+    assert torch.equal(E.H, H_eager)
+    assert E.H.sum().item() > 0
+    E.replay()  # a second replay gives the same again
+    torch.cuda.synchronize()
+    assert torch.equal(E.H, H_eager)
+
+
+def test_autotune_picks_a_candidate_and_caches(cuda, tmp_path):
+    from turbulence_tracing_gb300 import autotune
+
+    ne, x = R.workload_density(32, 1e-3, -11 / 3, 0.2, 1e24, 1)
+    s0 = R.gaussian_beam(3000, 0.25e-3, 5e-5, x.max(), np.random.default_rng(0))
+    cache = str(tmp_path / "tune.json")
+    r1 = autotune.tune(ne, x, x, x, s0, R.t_end(x.max()), x.max(), lwl=LWL, blocks=(64, 128),
+                       brick_depths=(8, 16), cache_file=cache, force=True)
+    assert r1["block"] in (64, 128) and r1["brick_depth"] in (8, 16)
+    assert len(r1["ms"]) == 4 and all(v > 0 for v in r1["ms"].values())
+    r2 = autotune.tune(ne, x, x, x, s0, R.t_end(x.max()), x.max(), lwl=LWL, cache_file=cache)
+    assert r2 == r1

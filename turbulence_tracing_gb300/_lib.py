@@ -33,6 +33,7 @@ OPTIC_RECT_APERTURE = 5
 OPTIC_KNIFE_EDGE = 6
 OPTIC_M_TO_MM = 7
 MAX_OPTICS = 64
+MAX_INSTANCES = 128
 
 
 class TTError(RuntimeError):
@@ -45,14 +46,14 @@ class TTError(RuntimeError):
 
 class TTVolume(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int32 * 3), ("axis", ctypes.c_int32 * 3), ("tiles", ctypes.c_int32 * 2),
-                ("supertiles", ctypes.c_int32 * 2), ("bricks_c", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("supertiles", ctypes.c_int32 * 2), ("bricks_c", ctypes.c_int32), ("brick_depth", ctypes.c_int32),
                 ("origin", ctypes.c_double * 3), ("spacing", ctypes.c_double * 3), ("omega", ctypes.c_double),
                 ("ne_max", ctypes.c_double), ("n_float4", ctypes.c_int64), ("nodes", ctypes.c_void_p)]
 
 
 class TTTraceOpts(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double), ("atol_phase", ctypes.c_double),
-                ("max_steps", ctypes.c_int64), ("with_phase", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("max_steps", ctypes.c_int64), ("with_phase", ctypes.c_int32), ("block_size", ctypes.c_int32)]
 
 
 class TTOptic(ctypes.Structure):
@@ -75,6 +76,7 @@ SIGNATURES = {
                         c_void_p, c_i64, c_void_p, c_void_p]),
     "tt_volume_plan": (c_int, [c_int, c_int, c_int, c_double_p, c_double_p, c_double_p, c_int,
                                ctypes.c_double, ctypes.c_double, ctypes.POINTER(TTVolume)]),
+    "tt_volume_set_brick_depth": (c_int, [ctypes.POINTER(TTVolume), c_int]),
     "tt_volume_build": (c_int, [ctypes.POINTER(TTVolume), c_void_p, c_int, c_void_p]),
     "tt_trace_f64": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p,
                              c_void_p, ctypes.c_double, c_void_p, c_i64, ctypes.c_double, c_int,
@@ -84,6 +86,10 @@ SIGNATURES = {
     "tt_trace_f32": (c_int, [ctypes.POINTER(TTVolume), c_void_p, c_i64, ctypes.c_double, ctypes.c_double,
                              ctypes.POINTER(TTTraceOpts), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                              c_void_p, c_size, c_void_p]),
+    "tt_trace_f32_batched_workspace_bytes": (c_size, [ctypes.POINTER(TTVolume), c_int, c_i64]),
+    "tt_trace_f32_batched": (c_int, [ctypes.POINTER(TTVolume), c_int, ctypes.POINTER(c_i64), c_double_p, c_double_p,
+                                     c_void_p, ctypes.POINTER(TTTraceOpts), c_void_p, c_void_p, c_void_p,
+                                     c_void_p, c_void_p, c_void_p, c_size, c_void_p]),
     "tt_detect": (c_int, [c_void_p, c_i64, ctypes.POINTER(TTOptic), c_int, c_int, c_int, ctypes.c_double,
                           ctypes.c_double, ctypes.c_double, ctypes.c_double, c_void_p, c_void_p, c_void_p,
                           c_void_p, c_int, c_void_p]),

@@ -131,28 +131,42 @@ class Volume32:
         return self.nodes.numel() * self.nodes.element_size()
 
 
-def build_volume(ne, x, y, z, probing_axis=2, lwl=1053e-9, ne_max=1.0):
-    """K1 FP32: write the brick-tiled node volume from a density (numpy or tensor)."""
+def build_volume(ne, x, y, z, probing_axis=2, lwl=1053e-9, ne_max=1.0, brick_depth=8, nodes=None):
+    """K1 FP32: write the brick-tiled node volume from a density (numpy or tensor).
+    brick_depth: nodes per brick along the probing axis (4, 8, 16 or 32)."""
     dev = require_cuda()
     L = _lib.lib()
     ne_t = _dens_dev(ne, dev)
     desc = volume_plan(tuple(ne_t.shape), x, y, z, probing_axis, lwl, ne_max)
-    nodes = torch.empty((desc.n_float4, 4), dtype=torch.float32, device=dev)
+    if brick_depth != desc.brick_depth:
+        check(L.tt_volume_set_brick_depth(ctypes.byref(desc), int(brick_depth)), "tt_volume_set_brick_depth")
+    if nodes is None or nodes.numel() < desc.n_float4 * 4:
+        nodes = torch.empty((desc.n_float4, 4), dtype=torch.float32, device=dev)
     desc.nodes = nodes.data_ptr()
     check(L.tt_volume_build(ctypes.byref(desc), _ptr(ne_t), _dtype_code(ne_t), _stream()), "tt_volume_build")
-    return Volume32(desc, nodes)
+    vol = Volume32(desc, nodes)
+    vol.density = ne_t  # kept so rebuilding (rebuild_volume) needs no host round trip
+    return vol
+
+
+def rebuild_volume(vol):
+    """Re-run K1 into the existing node buffer (enqueue only: graph-capturable)."""
+    L = _lib.lib()
+    check(L.tt_volume_build(ctypes.byref(vol.desc), _ptr(vol.density), _dtype_code(vol.density), _stream()),
+          "tt_volume_build")
 
 
 # ---------------------------------------------------------------------------
 # K2
 # ---------------------------------------------------------------------------
-def _opts(rtol, atol, atol_phase, max_steps, with_phase):
+def _opts(rtol, atol, atol_phase, max_steps, with_phase, block_size=0):
     o = _lib.TTTraceOpts()
     o.rtol = float(rtol)
     o.atol = float(atol)
     o.atol_phase = float(atol_phase)
     o.max_steps = int(max_steps or 0)
     o.with_phase = 1 if with_phase else 0
+    o.block_size = int(block_size or 0)
     return o
 
 
@@ -185,7 +199,7 @@ def trace_f64(fields, s0, t_end, probing_axis, extent, rtol=1e-3, atol=1e-6, pha
 
 
 def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, phase=False, max_steps=None,
-              want_sf=True, ws=None, out=None):
+              want_sf=True, ws=None, out=None, block_size=0):
     """Persistent FP32 tracer over a Volume32.  s0: (6, Np) float64."""
     dev = require_cuda()
     L = _lib.lib()
@@ -198,13 +212,58 @@ def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, pha
     need = L.tt_trace_f32_workspace_bytes(ctypes.byref(vol.desc), np_)
     if ws is None or ws.numel() < need:
         ws = workspace(need, dev)
-    o = _opts(rtol, atol, atol_phase, max_steps, phase)
+    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size)
     check(L.tt_trace_f32(ctypes.byref(vol.desc), _ptr(s0_t), np_, float(t_end), float(extent), ctypes.byref(o),
                          _ptr(out["sf"]), _ptr(out["rf"]), _ptr(out["phase"]) if phase else None,
                          _ptr(out["status"]), _ptr(out["nsteps"]), _ptr(ws), ws.numel(), _stream()),
           "tt_trace_f32")
     out["_ws"] = ws
     return out
+
+
+def trace_f32_batched(vols, s0, ray_offsets, t_ends, extents, rtol=1e-7, atol=1e-5, atol_phase=1e-5,
+                      phase=False, max_steps=None, want_sf=True, ws=None, out=None, block_size=0):
+    """All instances in one persistent launch.  s0 is the instance-blocked ray
+    array: a flat float64 tensor holding instance i's (6, n_i) block at
+    6 * ray_offsets[i].  Outputs are blocked the same way (see ray_block)."""
+    dev = require_cuda()
+    L = _lib.lib()
+    n = len(vols)
+    if not (1 <= n <= _lib.MAX_INSTANCES):
+        raise ValueError("1..%d instances per launch" % _lib.MAX_INSTANCES)
+    offs = np.ascontiguousarray(np.asarray(ray_offsets, dtype=np.int64))
+    ntot = int(offs[-1])
+    s0_t = s0 if isinstance(s0, torch.Tensor) and s0.is_cuda else torch.as_tensor(np.asarray(s0), device=dev)
+    s0_t = s0_t.reshape(-1)
+    if s0_t.dtype != torch.float64 or s0_t.numel() != 6 * ntot:
+        raise ValueError("s0 must hold 6 * ray_offsets[-1] float64 values")
+    descs = (_lib.TTVolume * n)(*[v.desc for v in vols])
+    te = np.ascontiguousarray(np.asarray(t_ends, dtype=np.float64))
+    ex = np.ascontiguousarray(np.asarray(extents, dtype=np.float64))
+    if out is None:
+        out = dict(sf=torch.empty(6 * ntot, dtype=torch.float64, device=dev) if want_sf else None,
+                   rf=torch.empty(4 * ntot, dtype=torch.float64, device=dev),
+                   phase=torch.empty(ntot, dtype=torch.float64, device=dev),
+                   status=torch.empty(ntot, dtype=torch.int32, device=dev),
+                   nsteps=torch.empty(ntot, dtype=torch.int32, device=dev))
+    need = L.tt_trace_f32_batched_workspace_bytes(descs, n, ntot)
+    if ws is None or ws.numel() < need:
+        ws = workspace(need, dev)
+    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size)
+    dp = ctypes.POINTER(ctypes.c_double)
+    check(L.tt_trace_f32_batched(descs, n, offs.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), te.ctypes.data_as(dp),
+                                 ex.ctypes.data_as(dp), _ptr(s0_t), ctypes.byref(o), _ptr(out["sf"]), _ptr(out["rf"]),
+                                 _ptr(out["phase"]) if phase else None, _ptr(out["status"]), _ptr(out["nsteps"]),
+                                 _ptr(ws), ws.numel(), _stream()), "tt_trace_f32_batched")
+    out["_ws"] = ws
+    out["_keep"] = (descs, offs, te, ex)
+    return out
+
+
+def ray_block(flat, rows, ray_offsets, i):
+    """Instance i's (rows, n_i) view of an instance-blocked array."""
+    b, e = int(ray_offsets[i]), int(ray_offsets[i + 1])
+    return flat[rows * b:rows * e].view(rows, e - b)
 
 
 # ---------------------------------------------------------------------------

@@ -286,6 +286,8 @@ struct VolGeom {
     int tiles[2];
     int st[2];
     int bricks_c;
+    int bd;             // nodes per brick along c
+    int brick_f4;       // float4 per brick (25 bd)
     long long tile_f4;  // float4 per tile column
     float inv_nc;
     float q_max;        // ne_max
@@ -327,16 +329,16 @@ __global__ void volume_build_kernel(const T* __restrict__ ne, VolGeom g, long lo
          li += (long long)gridDim.x * blockDim.x) {
         const long long tile = li / g.tile_f4;
         const int within = (int)(li - tile * g.tile_f4);
-        const int brick = within / 200;
-        const int r = within - brick * 200;
-        const int al = r / 40;
-        const int bl = (r / 8) % 5;
-        const int cl = r & 7;
+        const int brick = within / g.brick_f4;
+        const int r = within - brick * g.brick_f4;
+        const int al = r / (5 * g.bd);
+        const int bl = (r / g.bd) % 5;
+        const int cl = r & (g.bd - 1);
         const long long st = tile >> 6;
         const uint32_t m = (uint32_t)(tile & 63);
         const int ta = (int)(st / g.st[1]) * 8 + (int)compact3(m);
         const int tb = (int)(st % g.st[1]) * 8 + (int)compact3(m >> 1);
-        const int a = ta * 4 + al, b = tb * 4 + bl, c = brick * 8 + cl;
+        const int a = ta * 4 + al, b = tb * 4 + bl, c = brick * g.bd + cl;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
         if (a < g.n[0] && b < g.n[1] && c < g.n[2]) {
             const size_t base = (size_t)a * g.strides[0] + (size_t)b * g.strides[1] + (size_t)c * g.strides[2];
@@ -392,13 +394,25 @@ extern "C" int tt_volume_plan(int nx, int ny, int nz, const double* x_host, cons
         v.tiles[i] = (cells + 3) / 4;
         v.supertiles[i] = (v.tiles[i] + 7) / 8;
     }
-    v.bricks_c = (v.n[2] + 7) / 8;
-    v.reserved = 0;
+    v.brick_depth = 8;
+    v.bricks_c = (v.n[2] + v.brick_depth - 1) / v.brick_depth;
     v.omega = (2.0 * M_PI) * (TT_C_LIGHT / lwl);
     v.ne_max = ne_max;
-    v.n_float4 = (int64_t)v.supertiles[0] * v.supertiles[1] * 64 * (int64_t)v.bricks_c * 200;
+    v.n_float4 = (int64_t)v.supertiles[0] * v.supertiles[1] * 64 * (int64_t)v.bricks_c * 25 * v.brick_depth;
     v.nodes = nullptr;
     *vol = v;
+    return TT_OK;
+}
+
+extern "C" int tt_volume_set_brick_depth(tt_volume* vol, int brick_depth)
+{
+    if (!vol) return tt::invalid("volume_set_brick_depth: null volume");
+    if (brick_depth < 4 || brick_depth > 32 || (brick_depth & (brick_depth - 1)) != 0)
+        return tt::invalid("volume_set_brick_depth: depth must be 4, 8, 16 or 32");
+    vol->brick_depth = brick_depth;
+    vol->bricks_c = (vol->n[2] + brick_depth - 1) / brick_depth;
+    vol->n_float4 = (int64_t)vol->supertiles[0] * vol->supertiles[1] * 64 * (int64_t)vol->bricks_c * 25 * brick_depth;
+    vol->nodes = nullptr;
     return TT_OK;
 }
 
@@ -425,8 +439,12 @@ extern "C" int tt_volume_build(const tt_volume* vol, const void* ne, int ne_dtyp
     g.tiles[1] = vol->tiles[1];
     g.st[0] = vol->supertiles[0];
     g.st[1] = vol->supertiles[1];
+    if (vol->brick_depth < 4 || vol->brick_depth > 32 || (vol->brick_depth & (vol->brick_depth - 1)) != 0)
+        return tt::invalid("volume_build: bad brick_depth (use tt_volume_plan / tt_volume_set_brick_depth)");
     g.bricks_c = vol->bricks_c;
-    g.tile_f4 = (long long)vol->bricks_c * 200;
+    g.bd = vol->brick_depth;
+    g.brick_f4 = 25 * vol->brick_depth;
+    g.tile_f4 = (long long)vol->bricks_c * g.brick_f4;
     g.inv_nc = (float)(1.0 / nc);
     g.q_max = (float)vol->ne_max;
     g.ne_clip = (float)(vol->ne_max * nc);

@@ -1,4 +1,4 @@
-// K2b: persistent FP32 tracer over the brick-tiled node volume.
+// K2b: persistent FP32 tracer over brick-tiled node volumes (one, or a batch).
 //
 // Same ODE as ElectronCube.solve/dsdt/dndr (particle_tracking/particle_tracker.py:
 // 243-256, 312-331, 398-419) in normalised variables:
@@ -7,22 +7,26 @@
 //   dP/dsigma = r u   (r = spacing_c / spacing_axis),
 //   du/dsigma = H(P)  (H = -0.5 d(ne_nc)/dx * spacing_c, trilinear in the cell),
 //   dphi/dsigma = kappa (n - 1) |u|, n - 1 = -q / (1 + sqrt(1 - q)), kappa = k0 spacing_c.
-// Each Dormand-Prince 5(4) step is clipped to end just past the next cell face,
-// so all seven stages evaluate one cell's trilinear polynomial (loaded once,
-// 8 float4 nodes) and the step never straddles a kink of the interpolant.
-// The face of the box is hit exactly (the field jumps to 0 outside, as
-// RegularGridInterpolator's fill_value=0).  Outside the box the ray is a
+// Each Dormand-Prince 5(4) step is aimed at the cell's next face (predicted
+// from position, velocity and acceleration), so all seven stages evaluate one
+// cell's trilinear polynomial (8 float4 nodes loaded once) and the kinks of
+// the interpolant sit at step ends.  A stage that leaves the cell is looked up
+// exactly (neighbour cell, or the fill value 0 beyond the box, as
+// RegularGridInterpolator's fill_value=0), and a step that runs too far past
+// a face is redone ending at the crossing.  Outside the box the ray is a
 // straight line, finished analytically.  Error control per ray (scipy's
-// controller constants) on position (cells), velocity and phase.
-// Position fraction, path length and phase are compensated sums.
+// controller constants) on position (cells), direction and phase.  Path
+// length and phase are compensated sums.
 //
-// Work distribution: rays are bucketed by the 4x4-cell tile they start in
-// (Morton order inside 8x8 super-tiles, the volume's own tile order), then a
-// persistent grid (one wave of resident blocks) pulls rays from that order
-// through a global work counter; each warp refills its finished lanes with one
-// warp-aggregated atomic (ballot / popc), so lanes stay busy while rays with
-// long and short paths mix.
+// Work distribution: rays are bucketed by (instance, the 4x4-cell tile they
+// start in) -- the volume's own tile order -- then a persistent grid of
+// resident blocks pulls them through one global work counter; each warp
+// refills its finished lanes with one warp-aggregated atomic (ballot / popc),
+// so lanes stay busy while rays with long and short paths mix.  In the batched
+// form each lane carries its ray's instance and reads that instance's
+// geometry from a shared-memory copy of the instance table.
 #include <math.h>
+#include <stddef.h>
 
 #include "tt_common.cuh"
 
@@ -78,38 +82,56 @@ Tab make_tab()
     return t;
 }
 
-struct Vol32 {
-    const float4* __restrict__ nodes;
-    int n[3];
-    int st_b;
-    long long tile_f4;
-    float r[3];
+// Geometry of one volume instance.
+struct Geo {
+    const float4* nodes;
+    long long tile_f4;    // float4 per tile column
+    long long ray_begin;  // first ray of this instance (its arrays are the blocks starting there)
+    long long nrays;      // rays of this instance
     double origin[3];
     double spacing[3];
     double inv_spacing[3];
-    int axis[3];
-    float kappa;
     double sig_end;
-    float sig_end_f;   // the same in FP32 for the step loop (no FP64 in the hot loop)
-    double t_end;
     double extent;
-    float rtol, atol_cells, atol_phase, inv_rtol, inv_atol_cells;
+    int n[3];
+    int axis[3];
+    int st_b;
+    int bd;               // nodes per brick along c
+    int bd_shift;
+    int brick_f4;         // float4 per brick (25 bd)
+    int bin_base;         // first bucket of this instance
+    float r[3];
+    float kappa;
+    float sig_end_f;      // sig_end in FP32 for the step loop (no FP64 in the hot loop)
+};
+
+// Controls shared by every instance.
+struct Ctl {
+    float rtol, inv_rtol, inv_atol_cells, atol_phase;
     int with_phase;
     long long max_steps;
 };
 
-__device__ inline long long tile_base(const Vol32& V, int ta, int tb)
+// Instance table, passed by value as a kernel parameter (so the launch can be
+// captured in a CUDA graph without any host-to-device copy).
+struct GeoTable {
+    int n;
+    Geo g[TT_MAX_INSTANCES];
+};
+static_assert(sizeof(GeoTable) < 30000, "instance table must fit in the kernel parameter space");
+
+__device__ __forceinline__ long long tile_base(const Geo& G, int ta, int tb)
 {
     const int sa = ta >> 3, sb = tb >> 3;
     const uint32_t m = spread3((uint32_t)(ta & 7)) | (spread3((uint32_t)(tb & 7)) << 1);
-    return ((long long)(sa * V.st_b + sb) * 64 + m) * V.tile_f4;
+    return ((long long)(sa * G.st_b + sb) * 64 + m) * G.tile_f4;
 }
 
-__device__ inline int tile_key(const Vol32& V, int ta, int tb)
+__device__ __forceinline__ int tile_key(const Geo& G, int ta, int tb)
 {
     const int sa = ta >> 3, sb = tb >> 3;
     const uint32_t m = spread3((uint32_t)(ta & 7)) | (spread3((uint32_t)(tb & 7)) << 1);
-    return (sa * V.st_b + sb) * 64 + (int)m;
+    return (sa * G.st_b + sb) * 64 + (int)m;
 }
 
 __device__ __forceinline__ float tri(const float* c, float fa, float fb, float fc)
@@ -125,7 +147,7 @@ __device__ __forceinline__ float tri(const float* c, float fa, float fb, float f
 
 // Polynomial coefficients of the trilinear interpolant of one component.
 __device__ __forceinline__ void poly(float v000, float v001, float v010, float v011, float v100, float v101,
-                            float v110, float v111, float* c)
+                                     float v110, float v111, float* c)
 {
     c[0] = v000;
     c[1] = v100 - v000;
@@ -137,22 +159,24 @@ __device__ __forceinline__ void poly(float v000, float v001, float v010, float v
     c[7] = ((v111 - v110) - (v101 - v100)) - ((v011 - v010) - (v001 - v000));
 }
 
-__device__ __forceinline__ void load_cell(const Vol32& V, long long tbase, int ca, int cb, int cc, float (*coef)[8])
+__device__ __forceinline__ void load_cell(const Geo& G, long long tbase, int ca, int cb, int cc, float (*coef)[8])
 {
-    const long long base = tbase + (long long)(cc >> 3) * 200 + ((ca & 3) * 5 + (cb & 3)) * 8 + (cc & 7);
-    const int dc = ((cc & 7) == 7) ? 193 : 1;
-    const float4* p = V.nodes + base;
+    const int cl = cc & (G.bd - 1);
+    const int dc = (cl == G.bd - 1) ? G.brick_f4 - (G.bd - 1) : 1;
+    const long long base = tbase + (long long)(cc >> G.bd_shift) * G.brick_f4 + ((ca & 3) * 5 + (cb & 3)) * G.bd + cl;
+    const float4* p = G.nodes + base;
+    const int db = G.bd, da = 5 * G.bd;
     const float4 n000 = __ldg(p), n001 = __ldg(p + dc);
-    const float4 n010 = __ldg(p + 8), n011 = __ldg(p + 8 + dc);
-    const float4 n100 = __ldg(p + 40), n101 = __ldg(p + 40 + dc);
-    const float4 n110 = __ldg(p + 48), n111 = __ldg(p + 48 + dc);
+    const float4 n010 = __ldg(p + db), n011 = __ldg(p + db + dc);
+    const float4 n100 = __ldg(p + da), n101 = __ldg(p + da + dc);
+    const float4 n110 = __ldg(p + da + db), n111 = __ldg(p + da + db + dc);
     poly(n000.x, n001.x, n010.x, n011.x, n100.x, n101.x, n110.x, n111.x, coef[0]);
     poly(n000.y, n001.y, n010.y, n011.y, n100.y, n101.y, n110.y, n111.y, coef[1]);
     poly(n000.z, n001.z, n010.z, n011.z, n100.z, n101.z, n110.z, n111.z, coef[2]);
     poly(n000.w, n001.w, n010.w, n011.w, n100.w, n101.w, n110.w, n111.w, coef[3]);
 }
 
-__device__ inline float nm1f(float q)
+__device__ __forceinline__ float nm1f(float q)
 {
     float r = 1.0f - q;
     r = r > 0.0f ? r : 0.0f;
@@ -160,7 +184,7 @@ __device__ inline float nm1f(float q)
 }
 
 // Neumaier summation s + x with running compensation c (no contraction).
-__device__ inline void neumaier(float& s, float& c, float x)
+__device__ __forceinline__ void neumaier(float& s, float& c, float x)
 {
     const float t = __fadd_rn(s, x);
     if (fabsf(s) >= fabsf(x)) c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, t), x));
@@ -209,7 +233,8 @@ __device__ __forceinline__ float first_hit(float v, float acc, float d)
 // ci + floor(P), used when a stage leaves the current cell.  Scalars in,
 // float4 {H_a, H_b, H_c, q} out, so the caller's stage arrays stay in registers.
 __device__ __noinline__ float4 eval_exact(const float4* __restrict__ nodes, int n0, int n1, int n2, int st_b,
-                                          long long tile_f4, int c0, int c1, int c2, float p0, float p1, float p2)
+                                          long long tile_f4, int bd, int bd_shift, int brick_f4, int c0, int c1,
+                                          int c2, float p0, float p1, float p2)
 {
     const int n[3] = {n0, n1, n2};
     int c[3] = {c0, c1, c2};
@@ -231,13 +256,15 @@ __device__ __noinline__ float4 eval_exact(const float4* __restrict__ nodes, int 
     const int ta = c[0] >> 2, tb = c[1] >> 2;
     const uint32_t m = spread3((uint32_t)(ta & 7)) | (spread3((uint32_t)(tb & 7)) << 1);
     const long long tbase = ((long long)((ta >> 3) * st_b + (tb >> 3)) * 64 + m) * tile_f4;
-    const long long base = tbase + (long long)(c[2] >> 3) * 200 + ((c[0] & 3) * 5 + (c[1] & 3)) * 8 + (c[2] & 7);
-    const int dc = ((c[2] & 7) == 7) ? 193 : 1;
+    const int cl = c[2] & (bd - 1);
+    const int dc = (cl == bd - 1) ? brick_f4 - (bd - 1) : 1;
+    const long long base = tbase + (long long)(c[2] >> bd_shift) * brick_f4 + ((c[0] & 3) * 5 + (c[1] & 3)) * bd + cl;
     const float4* p = nodes + base;
+    const int db = bd, da = 5 * bd;
     const float4 n000 = __ldg(p), n001 = __ldg(p + dc);
-    const float4 n010 = __ldg(p + 8), n011 = __ldg(p + 8 + dc);
-    const float4 n100 = __ldg(p + 40), n101 = __ldg(p + 40 + dc);
-    const float4 n110 = __ldg(p + 48), n111 = __ldg(p + 48 + dc);
+    const float4 n010 = __ldg(p + db), n011 = __ldg(p + db + dc);
+    const float4 n100 = __ldg(p + da), n101 = __ldg(p + da + dc);
+    const float4 n110 = __ldg(p + da + db), n111 = __ldg(p + da + db + dc);
     const float fa = f[0], fb = f[1], fc = f[2];
 #define TT_LERP3(C)                                                                                  \
     fmaf(fa, fmaf(fb, fmaf(fc, n111.C - n110.C, n110.C) - fmaf(fc, n101.C - n100.C, n100.C),         \
@@ -255,7 +282,7 @@ __device__ __noinline__ float4 eval_exact(const float4* __restrict__ nodes, int 
 // kTolE of an interior face and moving through it is assigned to the cell it
 // enters; the upper box face belongs to the last cell.  Returns true when the
 // ray is outside the box.
-__device__ __forceinline__ bool renormalise(const Vol32& V, Ray& R)
+__device__ __forceinline__ bool renormalise(const Geo& G, Ray& R)
 {
     bool out = false;
 #pragma unroll
@@ -263,14 +290,14 @@ __device__ __forceinline__ bool renormalise(const Vol32& V, Ray& R)
         const float fl = floorf(R.fr[a]);
         int c = R.ci[a] + (int)fl;
         float f = R.fr[a] - fl;
-        if (c == V.n[a] - 1 && f == 0.f) {
-            c = V.n[a] - 2;
+        if (c == G.n[a] - 1 && f == 0.f) {
+            c = G.n[a] - 2;
             f = 1.f;
         }
         // pre-assign only when the face is within kFacePath of path ahead, so a
         // slow (grazing) ray never runs far on the next cell's polynomial
-        const float vel = V.r[a] * R.u[a];
-        if (vel > 0.f && 1.f - f < fminf(kTolE, kFacePath * vel) && c < V.n[a] - 2) {
+        const float vel = G.r[a] * R.u[a];
+        if (vel > 0.f && 1.f - f < fminf(kTolE, kFacePath * vel) && c < G.n[a] - 2) {
             c += 1;
             f -= 1.f;
         } else if (vel < 0.f && f < fminf(kTolE, -kFacePath * vel) && c > 0) {
@@ -280,32 +307,35 @@ __device__ __forceinline__ bool renormalise(const Vol32& V, Ray& R)
         if (c != R.ci[a]) R.cell_dirty = true;
         R.ci[a] = c;
         R.fr[a] = f;
-        out = out || c < 0 || c > V.n[a] - 2;
+        out = out || c < 0 || c > G.n[a] - 2;
     }
     return out;
 }
 
 // Initialise from s0 (SI units, physical axes).  Returns false when the ray
 // never enters the box before t_end (straight line throughout).
-__device__ __forceinline__ bool init_ray(const Vol32& V, const double* __restrict__ s0, long long np, long long r, Ray& R,
-                         double P[3], double uu[3])
+__device__ __forceinline__ bool init_ray(const Geo& G, const double* __restrict__ s0, long long np, long long r,
+                                         Ray& R, double P[3], double uu[3])
 {
+    // instance-blocked arrays: this instance's s0 is (6, nrays) at 6 * ray_begin
+    const double* s = s0 + 6 * G.ray_begin;
+    const long long lr = r - G.ray_begin, ln = G.nrays;
     double x[3], v[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        x[i] = s0[(size_t)i * np + r];
-        v[i] = s0[(size_t)(3 + i) * np + r];
+        x[i] = s[(size_t)i * ln + lr];
+        v[i] = s[(size_t)(3 + i) * ln + lr];
     }
     bool finite = true;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        P[a] = (x[V.axis[a]] - V.origin[a]) * V.inv_spacing[a];  // FP64 multiply, no divide
+        P[a] = (x[G.axis[a]] - G.origin[a]) * G.inv_spacing[a];  // FP64 multiply, no divide
         // a start on a box face (up to the rounding of this transform) is on it,
         // as RegularGridInterpolator counts the end coordinates as inside
-        const double hi = (double)(V.n[a] - 1);
+        const double hi = (double)(G.n[a] - 1);
         if (fabs(P[a]) < 1e-9) P[a] = 0.0;
         if (fabs(P[a] - hi) < 1e-9 * hi) P[a] = hi;
-        uu[a] = v[V.axis[a]] * (1.0 / TT_C_LIGHT);
+        uu[a] = v[G.axis[a]] * (1.0 / TT_C_LIGHT);
         finite = finite && isfinite(P[a]) && isfinite(uu[a]);
     }
     R.natt = R.nacc = 0;
@@ -323,15 +353,15 @@ __device__ __forceinline__ bool init_ray(const Vol32& V, const double* __restric
     }
     // slab test in sigma units (dP/dsigma = r u), FP32: rays that start inside
     // get tin = 0 exactly; for the others it places the entry point
-    float tin = 0.f, tout = V.sig_end_f;
+    float tin = 0.f, tout = G.sig_end_f;
     int enter_axis = -1;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const float vel = V.r[a] * (float)uu[a];
-        const float hi = (float)(V.n[a] - 1);
+        const float vel = G.r[a] * (float)uu[a];
+        const float hi = (float)(G.n[a] - 1);
         const float pa = (float)P[a];
         if (vel == 0.f) {
-            if (P[a] < 0.0 || P[a] > (double)(V.n[a] - 1)) tout = -1.f;
+            if (P[a] < 0.0 || P[a] > (double)(G.n[a] - 1)) tout = -1.f;
         } else {
             const float iv = 1.f / vel;
             float t1 = (0.f - pa) * iv, t2 = (hi - pa) * iv;
@@ -340,19 +370,19 @@ __device__ __forceinline__ bool init_ray(const Vol32& V, const double* __restric
             if (t2 < tout) tout = t2;
         }
     }
-    if (!(tin <= tout) || tin >= V.sig_end_f) {
+    if (!(tin <= tout) || tin >= G.sig_end_f) {
         R.state = 1;  // never inside: straight line
         R.sig = 0.f;
         return false;
     }
     double Pe[3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) Pe[a] = fma((double)V.r[a] * uu[a], (double)tin, P[a]);
-    if (enter_axis >= 0) Pe[enter_axis] = uu[enter_axis] > 0.0 ? 0.0 : (double)(V.n[enter_axis] - 1);
+    for (int a = 0; a < 3; ++a) Pe[a] = fma((double)G.r[a] * uu[a], (double)tin, P[a]);
+    if (enter_axis >= 0) Pe[enter_axis] = uu[enter_axis] > 0.0 ? 0.0 : (double)(G.n[enter_axis] - 1);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         double c = floor(Pe[a]);
-        if (c > V.n[a] - 2) c = V.n[a] - 2;
+        if (c > G.n[a] - 2) c = G.n[a] - 2;
         if (c < 0) c = 0;
         R.ci[a] = (int)c;
         R.fr[a] = (float)(Pe[a] - c);
@@ -368,9 +398,10 @@ __device__ __forceinline__ bool init_ray(const Vol32& V, const double* __restric
     return true;
 }
 
-__device__ __forceinline__ void finish_ray(const Vol32& V, const Ray& R, const double P0[3], const double u0[3], long long r,
-                           long long np, double* __restrict__ sf, double* __restrict__ rf,
-                           double* __restrict__ phase, int* __restrict__ status, int* __restrict__ nsteps)
+__device__ __forceinline__ void finish_ray(const Geo& G, const Ray& R, const double P0[3], const double u0[3],
+                                           long long r, long long np, double* __restrict__ sf,
+                                           double* __restrict__ rf, double* __restrict__ phase,
+                                           int* __restrict__ status, int* __restrict__ nsteps)
 {
     // Position/velocity where stepping stopped, then the straight-line flight to
     // t_end for rays outside the box (zero field there): rays that left the box,
@@ -383,37 +414,40 @@ __device__ __forceinline__ void finish_ray(const Vol32& V, const Ray& R, const d
             P[a] = (double)R.ci[a] + (double)R.fr[a];
             u[a] = (double)R.u[a];
         }
-        if (R.state == 1 && R.code == TT_RAY_OK) ds = V.sig_end - sig > 0.0 ? V.sig_end - sig : 0.0;
+        if (R.state == 1 && R.code == TT_RAY_OK) ds = G.sig_end - sig > 0.0 ? G.sig_end - sig : 0.0;
     } else {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             P[a] = P0[a];
             u[a] = u0[a];
         }
-        if (R.code == TT_RAY_OK) ds = V.sig_end;
+        if (R.code == TT_RAY_OK) ds = G.sig_end;
     }
 #pragma unroll
-    for (int a = 0; a < 3; ++a) P[a] += (double)V.r[a] * u[a] * ds;
+    for (int a = 0; a < 3; ++a) P[a] += (double)G.r[a] * u[a] * ds;
     double y[6];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        y[V.axis[a]] = V.origin[a] + P[a] * V.spacing[a];
-        y[3 + V.axis[a]] = u[a] * TT_C_LIGHT;
+        y[G.axis[a]] = G.origin[a] + P[a] * G.spacing[a];
+        y[3 + G.axis[a]] = u[a] * TT_C_LIGHT;
     }
+    const long long lr = r - G.ray_begin, ln = G.nrays;
     if (sf) {
+        double* o = sf + 6 * G.ray_begin;
 #pragma unroll
-        for (int i = 0; i < 6; ++i) sf[(size_t)i * np + r] = y[i];
+        for (int i = 0; i < 6; ++i) o[(size_t)i * ln + lr] = y[i];
     }
     if (rf) {
-        const int ax = V.axis[2];
+        double* o = rf + 4 * G.ray_begin;
+        const int ax = G.axis[2];
         const int p0 = ax == 0 ? 1 : 0, p1 = ax == 2 ? 1 : 2;
-        const double tbp = (y[ax] - V.extent) / y[3 + ax];
-        rf[r] = y[p0] - y[3 + p0] * tbp;
-        rf[(size_t)2 * np + r] = y[p1] - y[3 + p1] * tbp;
+        const double tbp = (y[ax] - G.extent) / y[3 + ax];
+        o[lr] = y[p0] - y[3 + p0] * tbp;
+        o[(size_t)2 * ln + lr] = y[p1] - y[3 + p1] * tbp;
         // angles from the FP32 direction the ray carries (relative error ~1e-7 of the angle)
         const float uc = (float)u[2];
-        rf[(size_t)np + r] = (double)atanf((float)y[3 + p0] * (1.f / 299792458.f) / uc);
-        rf[(size_t)3 * np + r] = (double)atanf((float)y[3 + p1] * (1.f / 299792458.f) / uc);
+        o[(size_t)ln + lr] = (double)atanf((float)y[3 + p0] * (1.f / 299792458.f) / uc);
+        o[(size_t)3 * ln + lr] = (double)atanf((float)y[3 + p1] * (1.f / 299792458.f) / uc);
     }
     if (phase) phase[r] = (double)R.ph + (double)R.phc;
     if (status) status[r] = R.code;
@@ -423,24 +457,24 @@ __device__ __forceinline__ void finish_ray(const Vol32& V, const Ray& R, const d
 // Right-hand side at stage position Ps (fractions in the current cell):
 // the current cell's polynomial while Ps stays within kTolE of it (never past
 // a box face), the exact lookup otherwise.
-__device__ __forceinline__ void stage_eval(const Vol32& V, const Ray& R, const float (*coef)[8], const float Ps[3],
-                                           float H[3], float& q)
+__device__ __forceinline__ void stage_eval(const Geo& G, const Ctl& K, const Ray& R, const float (*coef)[8],
+                                           const float Ps[3], float H[3], float& q)
 {
     bool home = true;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float lo = R.ci[a] == 0 ? 0.f : -kTolE;
-        const float hi = R.ci[a] == V.n[a] - 2 ? 1.f : 1.f + kTolE;
+        const float hi = R.ci[a] == G.n[a] - 2 ? 1.f : 1.f + kTolE;
         home = home && Ps[a] >= lo && Ps[a] <= hi;
     }
     if (home) {
         H[0] = tri(coef[0], Ps[0], Ps[1], Ps[2]);
         H[1] = tri(coef[1], Ps[0], Ps[1], Ps[2]);
         H[2] = tri(coef[2], Ps[0], Ps[1], Ps[2]);
-        q = V.with_phase ? tri(coef[3], Ps[0], Ps[1], Ps[2]) : 0.f;
+        q = K.with_phase ? tri(coef[3], Ps[0], Ps[1], Ps[2]) : 0.f;
     } else {
-        const float4 r = eval_exact(V.nodes, V.n[0], V.n[1], V.n[2], V.st_b, V.tile_f4, R.ci[0], R.ci[1], R.ci[2],
-                                    Ps[0], Ps[1], Ps[2]);
+        const float4 r = eval_exact(G.nodes, G.n[0], G.n[1], G.n[2], G.st_b, G.tile_f4, G.bd, G.bd_shift,
+                                    G.brick_f4, R.ci[0], R.ci[1], R.ci[2], Ps[0], Ps[1], Ps[2]);
         H[0] = r.x;
         H[1] = r.y;
         H[2] = r.z;
@@ -449,42 +483,42 @@ __device__ __forceinline__ void stage_eval(const Vol32& V, const Ray& R, const f
 }
 
 // One attempted step.  Returns with R updated.
-__device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float (*coef)[8])
+__device__ __forceinline__ void step(const Geo& G, const Ctl& K, const Tab& T, Ray& R, float (*coef)[8])
 {
     if (R.cell_dirty) {
         const int ta = R.ci[0] >> 2, tb = R.ci[1] >> 2;
         if (ta != R.ta || tb != R.tb) {
             R.ta = ta;
             R.tb = tb;
-            R.tbase = tile_base(V, ta, tb);
+            R.tbase = tile_base(G, ta, tb);
         }
-        load_cell(V, R.tbase, R.ci[0], R.ci[1], R.ci[2], coef);
+        load_cell(G, R.tbase, R.ci[0], R.ci[1], R.ci[2], coef);
         R.cell_dirty = false;
     }
-    const float rem = (V.sig_end_f - R.sig) - R.sigc;
+    const float rem = (G.sig_end_f - R.sig) - R.sigc;
     if (!(rem > 0.f)) {
         R.state = 2;
         return;
     }
-    if (R.natt >= V.max_steps) {
+    if (R.natt >= K.max_steps) {
         R.code = TT_RAY_MAX_STEPS;
         R.state = 3;
         return;
     }
     float Hs[7][3];
     float q0;
-    stage_eval(V, R, coef, R.fr, Hs[0], q0);
+    stage_eval(G, K, R, coef, R.fr, Hs[0], q0);
     // Predict the first face crossing of the cell from position, velocity and
     // acceleration; aim the step end at it.  Leaving through a box face within
     // kBoxPath: the ray has left (the field beyond is the fill value 0).
     float hf = 3.0e38f;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const float vel = V.r[a] * R.u[a];
-        const float acc = V.r[a] * Hs[0][a];
+        const float vel = G.r[a] * R.u[a];
+        const float acc = G.r[a] * Hs[0][a];
         const float hu = first_hit(vel, acc, 1.f - R.fr[a]);
         const float hl = first_hit(-vel, -acc, R.fr[a]);
-        const bool box_up = R.ci[a] == V.n[a] - 2, box_lo = R.ci[a] == 0;
+        const bool box_up = R.ci[a] == G.n[a] - 2, box_lo = R.ci[a] == 0;
         if ((box_up && vel > 0.f && (1.f - R.fr[a]) <= kBoxPath * vel) ||
             (box_lo && vel < 0.f && R.fr[a] <= -kBoxPath * vel)) {
             R.state = 1;
@@ -502,10 +536,10 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
     }
     float phb = 0.f, phe = 0.f;
     float Pn[3], un[3];
-    if (V.with_phase) {
+    if (K.with_phase) {
         const float u2 = fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2]));
         const float sp = u2 * rsqrtf(u2);
-        const float dph = V.kappa * nm1f(q0) * sp;
+        const float dph = G.kappa * nm1f(q0) * sp;
         phb = T.b[0] * dph;
         phe = T.e[0] * dph;
     }
@@ -521,14 +555,14 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
                 saa = fmaf(T.aa[s][k], Hs[k][c], saa);
             }
             us[c] = fmaf(h, sa, R.u[c]);
-            Ps[c] = fmaf(h * V.r[c], fmaf(T.cs[s], R.u[c], h * saa), R.fr[c]);
+            Ps[c] = fmaf(h * G.r[c], fmaf(T.cs[s], R.u[c], h * saa), R.fr[c]);
         }
         float q;
-        stage_eval(V, R, coef, Ps, Hs[s], q);
-        if (V.with_phase) {
+        stage_eval(G, K, R, coef, Ps, Hs[s], q);
+        if (K.with_phase) {
             const float u2 = fmaf(us[0], us[0], fmaf(us[1], us[1], us[2] * us[2]));
             const float sp = u2 * rsqrtf(u2);
-            const float dph = V.kappa * nm1f(q) * sp;
+            const float dph = G.kappa * nm1f(q) * sp;
             if (s < 6) phb = fmaf(T.b[s], dph, phb);
             phe = fmaf(T.e[s], dph, phe);
         }
@@ -544,7 +578,7 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
     // velocity tolerance is an angle
     const float q0u = fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2]));
     const float q1u = fmaf(un[0], un[0], fmaf(un[1], un[1], un[2] * un[2]));
-    const float inv_scu = rsqrtf(fmaxf(q0u, q1u)) * V.inv_rtol;  // 1 / (rtol |u|)
+    const float inv_scu = rsqrtf(fmaxf(q0u, q1u)) * K.inv_rtol;  // 1 / (rtol |u|)
     float es = 0.f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -554,17 +588,17 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
 #pragma unroll
         for (int k = 0; k < 6; ++k) ep = fmaf(T.ea[k], Hs[k][c], ep);
         eu *= h;
-        ep *= h * h * V.r[c];
+        ep *= h * h * G.r[c];
         const float x1 = eu * inv_scu;
-        const float x2 = ep * V.inv_atol_cells;
+        const float x2 = ep * K.inv_atol_cells;
         es = fmaf(x1, x1, fmaf(x2, x2, es));
     }
     int neq = 6;
     float dphi = 0.f;
-    if (V.with_phase) {
+    if (K.with_phase) {
         dphi = h * phb;
         const float phn = R.ph + dphi;
-        const float scp = V.atol_phase + V.rtol * fmaxf(fabsf(R.ph), fabsf(phn));
+        const float scp = K.atol_phase + K.rtol * fmaxf(fabsf(R.ph), fabsf(phn));
         const float x = __fdividef(h * phe, scp);
         es = fmaf(x, x, es);
         neq = 7;
@@ -590,12 +624,12 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
     float hre = 3.0e38f;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const float vend = V.r[a] * un[a];
+        const float vend = G.r[a] * un[a];
         float over = 0.f;  // path past the crossed face
         bool box = false;
         if (Pn[a] > 1.f && R.fr[a] <= 1.f) {
             over = __fdividef(Pn[a] - 1.f, fmaxf(vend, 1e-6f));
-            box = R.ci[a] == V.n[a] - 2;
+            box = R.ci[a] == G.n[a] - 2;
         } else if (Pn[a] < 0.f && R.fr[a] >= 0.f) {
             over = __fdividef(-Pn[a], fmaxf(-vend, 1e-6f));
             box = R.ci[a] == 0;
@@ -626,22 +660,34 @@ __device__ __forceinline__ void step(const Vol32& V, const Tab& T, Ray& R, float
         R.sigc = __fsub_rn(__fsub_rn(t, R.sig), y);
         R.sig = t;
     }
-    if (V.with_phase) neumaier(R.ph, R.phc, dphi);
-    if (renormalise(V, R)) R.state = 1;
+    if (K.with_phase) neumaier(R.ph, R.phc, dphi);
+    if (renormalise(G, R)) R.state = 1;
     else if (last) R.state = 2;
 }
 
-#ifndef TT_TRACE32_MIN_BLOCKS
-#define TT_TRACE32_MIN_BLOCKS 4
-#endif
-__global__ void __launch_bounds__(128, TT_TRACE32_MIN_BLOCKS)
-trace32_kernel(Vol32 V, Tab T, const double* __restrict__ s0, long long np,
-               const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
-               double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
-               int* __restrict__ status, int* __restrict__ nsteps)
+// Instance of ray r: the last instance whose ray_begin <= r.
+__device__ __forceinline__ int instance_of(const Geo* g, int n, long long r)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (g[mid].ray_begin <= r) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The persistent loop, shared by the single-volume and batched kernels.
+// GeoOf(r) returns the geometry of ray r's instance.
+template <typename GeoOf>
+__device__ __forceinline__ void persistent_loop(GeoOf geo_of, const Ctl& K, const Tab& T, const double* __restrict__ s0,
+                                                long long np, const unsigned* __restrict__ perm,
+                                                unsigned long long* __restrict__ counter, double* __restrict__ sf,
+                                                double* __restrict__ rf, double* __restrict__ phase,
+                                                int* __restrict__ status, int* __restrict__ nsteps)
 {
     const unsigned lane = threadIdx.x & 31u;
     long long idx = -1;      // position in perm of this lane's ray
+    long long ray = 0;
     bool drained = false;
     Ray R;
     double P0[3], u0[3];
@@ -659,9 +705,9 @@ trace32_kernel(Vol32 V, Tab T, const double* __restrict__ s0, long long np,
                 const unsigned long long my = base + __popc(mask & ((1u << lane) - 1u));
                 if (my < (unsigned long long)np) {
                     idx = (long long)my;
-                    const long long r = perm ? (long long)perm[idx] : idx;
-                    if (!init_ray(V, s0, np, r, R, P0, u0)) {
-                        finish_ray(V, R, P0, u0, r, np, sf, rf, phase, status, nsteps);
+                    ray = perm ? (long long)perm[idx] : idx;
+                    if (!init_ray(geo_of(ray), s0, np, ray, R, P0, u0)) {
+                        finish_ray(geo_of(ray), R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
                         idx = -1;  // picked up again on the next pass
                     }
                 } else {
@@ -672,35 +718,82 @@ trace32_kernel(Vol32 V, Tab T, const double* __restrict__ s0, long long np,
         const bool active = idx >= 0;
         if (__ballot_sync(0xffffffffu, active || (!drained)) == 0u) break;
         if (active) {
-            step(V, T, R, coef);
+            step(geo_of(ray), K, T, R, coef);
             if (R.state != 0) {
-                const long long r = perm ? (long long)perm[idx] : idx;
-                finish_ray(V, R, P0, u0, r, np, sf, rf, phase, status, nsteps);
+                finish_ray(geo_of(ray), R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
                 idx = -1;
             }
         }
     }
 }
 
-// --- ray bucketing by entry tile ----------------------------------------------
-__device__ inline int ray_key(const Vol32& V, const double* __restrict__ s0, long long np, long long r)
+struct SingleGeo {
+    const Geo* g;
+    __device__ __forceinline__ const Geo& operator()(long long) const { return *g; }
+};
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 512 / BLOCK)
+trace32_kernel(const Geo G, Ctl K, Tab T, const double* __restrict__ s0, long long np,
+               const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
+               double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
+               int* __restrict__ status, int* __restrict__ nsteps)
 {
-    const double xa = s0[(size_t)V.axis[0] * np + r];
-    const double xb = s0[(size_t)V.axis[1] * np + r];
-    double pa = (xa - V.origin[0]) / V.spacing[0];
-    double pb = (xb - V.origin[1]) / V.spacing[1];
-    if (!(pa >= 0.0)) pa = 0.0;  // NaN too
-    if (!(pb >= 0.0)) pb = 0.0;
-    int ca = pa > (double)(V.n[0] - 2) ? V.n[0] - 2 : (int)pa;
-    int cb = pb > (double)(V.n[1] - 2) ? V.n[1] - 2 : (int)pb;
-    return tile_key(V, ca >> 2, cb >> 2);
+    persistent_loop(SingleGeo{&G}, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps);
 }
 
-__global__ void bin_count_kernel(Vol32 V, const double* __restrict__ s0, long long np, unsigned* __restrict__ cnt)
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 512 / BLOCK)
+trace32_batched_kernel(const GeoTable table, Ctl K, Tab T, const double* __restrict__ s0, long long np,
+                       const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
+                       double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
+                       int* __restrict__ status, int* __restrict__ nsteps)
+{
+    __shared__ Geo sg[TT_MAX_INSTANCES];
+    const int ninst = table.n;
+    for (int i = threadIdx.x; i < ninst; i += BLOCK) sg[i] = table.g[i];
+    __syncthreads();
+    // a lane's instance is found once per fetched ray; the lane keeps a pointer
+    // to that instance's entry, so field reads are plain offset loads
+    struct BatchGeo {
+        const Geo* sg;
+        int n;
+        mutable long long last_ray;
+        mutable const Geo* cur;
+        __device__ __forceinline__ const Geo& operator()(long long r) const
+        {
+            if (r != last_ray) {
+                cur = sg + instance_of(sg, n, r);
+                last_ray = r;
+            }
+            return *cur;
+        }
+    };
+    persistent_loop(BatchGeo{sg, ninst, -1, sg}, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps);
+}
+
+// --- ray bucketing by (instance, entry tile) ----------------------------------
+__device__ __forceinline__ int ray_key(const Geo& G, const double* __restrict__ s0, long long np, long long r)
+{
+    const double* s = s0 + 6 * G.ray_begin;
+    const long long lr = r - G.ray_begin, ln = G.nrays;
+    const double xa = s[(size_t)G.axis[0] * ln + lr];
+    const double xb = s[(size_t)G.axis[1] * ln + lr];
+    double pa = (xa - G.origin[0]) * G.inv_spacing[0];
+    double pb = (xb - G.origin[1]) * G.inv_spacing[1];
+    if (!(pa >= 0.0)) pa = 0.0;  // NaN too
+    if (!(pb >= 0.0)) pb = 0.0;
+    int ca = pa > (double)(G.n[0] - 2) ? G.n[0] - 2 : (int)pa;
+    int cb = pb > (double)(G.n[1] - 2) ? G.n[1] - 2 : (int)pb;
+    return G.bin_base + tile_key(G, ca >> 2, cb >> 2);
+}
+
+__global__ void bin_count_kernel(const GeoTable table, const double* __restrict__ s0, long long np,
+                                 unsigned* __restrict__ cnt)
 {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < np;
          r += (long long)gridDim.x * blockDim.x) {
-        const int key = ray_key(V, s0, np, r);
+        const int key = ray_key(table.g[instance_of(table.g, table.n, r)], s0, np, r);
         const unsigned peers = __match_any_sync(__activemask(), key);
         const int leader = __ffs(peers) - 1;
         if ((int)(threadIdx.x & 31u) == leader) atomicAdd(cnt + key, (unsigned)__popc(peers));
@@ -732,12 +825,12 @@ __global__ void bin_scan_kernel(unsigned* __restrict__ cnt, int n)
     }
 }
 
-__global__ void bin_scatter_kernel(Vol32 V, const double* __restrict__ s0, long long np,
+__global__ void bin_scatter_kernel(const GeoTable table, const double* __restrict__ s0, long long np,
                                    unsigned* __restrict__ cursor, unsigned* __restrict__ perm)
 {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < np;
          r += (long long)gridDim.x * blockDim.x) {
-        const int key = ray_key(V, s0, np, r);
+        const int key = ray_key(table.g[instance_of(table.g, table.n, r)], s0, np, r);
         const unsigned peers = __match_any_sync(__activemask(), key);
         const int leader = __ffs(peers) - 1;
         unsigned base = 0;
@@ -748,34 +841,153 @@ __global__ void bin_scatter_kernel(Vol32 V, const double* __restrict__ s0, long 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Host side
+int make_geo(const tt_volume* vol, double t_end, double extent, long long ray_begin, long long nrays, int bin_base,
+             Geo* out)
+{
+    if (!vol->nodes) return tt::invalid("trace_f32: volume has no node buffer");
+    for (int i = 0; i < 3; ++i)
+        if (vol->n[i] < 2) return tt::invalid("trace_f32: volume axis with < 2 nodes");
+    const int bd = vol->brick_depth;
+    if (bd < 4 || bd > 32 || (bd & (bd - 1)) != 0) return tt::invalid("trace_f32: bad brick_depth");
+    if (!(t_end >= 0.0)) return tt::invalid("trace_f32: t_end must be >= 0");
+    Geo G;
+    G.nodes = static_cast<const float4*>(vol->nodes);
+    for (int i = 0; i < 3; ++i) {
+        G.n[i] = vol->n[i];
+        G.origin[i] = vol->origin[i];
+        G.spacing[i] = vol->spacing[i];
+        G.inv_spacing[i] = 1.0 / vol->spacing[i];
+        G.axis[i] = vol->axis[i];
+        G.r[i] = (float)(vol->spacing[2] / vol->spacing[i]);
+    }
+    G.st_b = vol->supertiles[1];
+    G.bd = bd;
+    G.bd_shift = __builtin_ctz((unsigned)bd);
+    G.brick_f4 = 25 * bd;
+    G.tile_f4 = (long long)vol->bricks_c * G.brick_f4;
+    if ((long long)vol->supertiles[0] * vol->supertiles[1] * 64 * G.tile_f4 != vol->n_float4)
+        return tt::invalid("trace_f32: volume descriptor is inconsistent (use tt_volume_plan)");
+    G.kappa = (float)(vol->omega / TT_C_LIGHT * vol->spacing[2]);
+    G.sig_end = t_end * TT_C_LIGHT / vol->spacing[2];
+    G.sig_end_f = (float)G.sig_end;
+    G.extent = extent;
+    G.ray_begin = ray_begin;
+    G.nrays = nrays;
+    G.bin_base = bin_base;
+    *out = G;
+    return TT_OK;
+}
+
+int make_ctl(const tt_trace_opts* opts, Ctl* K)
+{
+    if (!(opts->rtol > 0.0) || !(opts->atol > 0.0))
+        return tt::invalid("trace_f32: need rtol > 0 and atol > 0 (cells)");
+    if (opts->with_phase && !(opts->atol_phase > 0.0)) return tt::invalid("trace_f32: need atol_phase > 0");
+    const int bs = opts->block_size;
+    if (bs != 0 && bs != 64 && bs != 128 && bs != 256)
+        return tt::invalid("trace_f32: block_size must be 64, 128 or 256");
+    K->rtol = (float)opts->rtol;
+    K->inv_rtol = (float)(1.0 / opts->rtol);
+    K->inv_atol_cells = (float)(1.0 / opts->atol);
+    K->atol_phase = (float)(opts->with_phase ? opts->atol_phase : 1.0);
+    K->with_phase = opts->with_phase ? 1 : 0;
+    K->max_steps = opts->max_steps > 0 ? opts->max_steps : TT_DEFAULT_MAX_STEPS;
+    return TT_OK;
+}
+
+int vol_bins(const tt_volume* vol) { return vol->supertiles[0] * vol->supertiles[1] * 64; }
+
 struct WsLayout {
     size_t counter_off, cnt_off, perm_off, total;
     int nbins;
 };
 
-WsLayout ws_layout(const tt_volume* vol, long long np)
+WsLayout ws_layout(int nbins, long long np)
 {
     WsLayout L;
-    L.nbins = vol->supertiles[0] * vol->supertiles[1] * 64;
+    L.nbins = nbins;
     L.counter_off = 0;
     L.cnt_off = 256;
-    L.perm_off = tt::align_up(L.cnt_off + sizeof(unsigned) * (size_t)L.nbins, 256);
+    L.perm_off = tt::align_up(L.cnt_off + sizeof(unsigned) * (size_t)nbins, 256);
     L.total = tt::align_up(L.perm_off + sizeof(unsigned) * (size_t)np, 256);
     return L;
 }
 
-int occupancy_grid()
+template <typename KernelT>
+int occupancy_grid(KernelT kernel, int block, int slot)
 {
-    static int blocks_per_sm[64] = {0};
+    static int cache[6][64] = {{0}};
     int dev = 0;
     cudaGetDevice(&dev);
-    int b = (dev >= 0 && dev < 64) ? blocks_per_sm[dev] : 0;
+    int b = (dev >= 0 && dev < 64) ? cache[slot][dev] : 0;
     if (b <= 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace32_kernel, 128, 0) != cudaSuccess || b < 1)
-            b = 1;
-        if (dev >= 0 && dev < 64) blocks_per_sm[dev] = b;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, block, 0) != cudaSuccess || b < 1) b = 1;
+        if (dev >= 0 && dev < 64) cache[slot][dev] = b;
     }
     return b * tt::sm_count();
+}
+
+const Tab& tableau()
+{
+    static const Tab T = make_tab();
+    return T;
+}
+
+int bin_grid(long long np)
+{
+    long long g = (np + 255) / 256;
+    const long long cap = (long long)tt::sm_count() * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+// Bucket, then trace.  table.n == 1 runs the single-volume kernel.
+int run(const GeoTable& table, int nbins, const Ctl& K, int block, const double* s0, long long np, double* sf,
+        double* rf, double* phase, int* status, int* nsteps, void* workspace, size_t workspace_bytes,
+        cudaStream_t s, const char* who)
+{
+    const WsLayout L = ws_layout(nbins, np);
+    if (!workspace || workspace_bytes < L.total) {
+        tt::set_detail("%s: workspace needs %zu bytes", who, L.total);
+        return TT_ERR_WORKSPACE_TOO_SMALL;
+    }
+    char* ws = static_cast<char*>(workspace);
+    unsigned long long* counter = reinterpret_cast<unsigned long long*>(ws + L.counter_off);
+    unsigned* cnt = reinterpret_cast<unsigned*>(ws + L.cnt_off);
+    unsigned* perm = reinterpret_cast<unsigned*>(ws + L.perm_off);
+    TT_TRY(tt::cuda_status(cudaMemsetAsync(ws, 0, L.perm_off, s), "trace_f32 workspace clear"));
+    bin_count_kernel<<<bin_grid(np), 256, 0, s>>>(table, s0, np, cnt);
+    bin_scan_kernel<<<1, 1024, 0, s>>>(cnt, nbins);
+    bin_scatter_kernel<<<bin_grid(np), 256, 0, s>>>(table, s0, np, cnt, perm);
+    TT_TRY(tt::launch_status("trace_f32 ray binning"));
+    const Tab& T = tableau();
+#define TT_LAUNCH_SINGLE(BS, SLOT)                                                                    \
+    trace32_kernel<BS><<<occupancy_grid(trace32_kernel<BS>, BS, SLOT), BS, 0, s>>>(                  \
+        table.g[0], K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
+#define TT_LAUNCH_BATCH(BS, SLOT)                                                                     \
+    trace32_batched_kernel<BS><<<occupancy_grid(trace32_batched_kernel<BS>, BS, SLOT), BS, 0, s>>>(  \
+        table, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
+    if (table.n == 1) {
+        if (block == 64) TT_LAUNCH_SINGLE(64, 0);
+        else if (block == 256) TT_LAUNCH_SINGLE(256, 2);
+        else TT_LAUNCH_SINGLE(128, 1);
+    } else {
+        if (block == 64) TT_LAUNCH_BATCH(64, 3);
+        else if (block == 256) TT_LAUNCH_BATCH(256, 5);
+        else TT_LAUNCH_BATCH(128, 4);
+    }
+#undef TT_LAUNCH_SINGLE
+#undef TT_LAUNCH_BATCH
+    return tt::launch_status("trace_f32 kernel");
+}
+
+GeoTable& host_table()
+{
+    static thread_local GeoTable t;
+    return t;
 }
 
 }  // namespace
@@ -783,7 +995,7 @@ int occupancy_grid()
 extern "C" size_t tt_trace_f32_workspace_bytes(const tt_volume* vol, int64_t np)
 {
     if (!vol || np < 0) return 0;
-    return ws_layout(vol, np).total;
+    return ws_layout(vol_bins(vol), np).total;
 }
 
 extern "C" int tt_trace_f32(const tt_volume* vol, const double* s0, int64_t np, double t_end, double extent,
@@ -791,61 +1003,54 @@ extern "C" int tt_trace_f32(const tt_volume* vol, const double* s0, int64_t np, 
                             int32_t* nsteps, void* workspace, size_t workspace_bytes, void* stream)
 {
     if (!vol || !opts) return tt::invalid("trace_f32: null volume or opts");
-    if (!vol->nodes) return tt::invalid("trace_f32: volume has no node buffer");
     if (np < 0) return tt::invalid("trace_f32: np < 0");
     if (np > 0xffffffffLL) return tt::invalid("trace_f32: at most 2^32-1 rays per call");
-    if (!(t_end >= 0.0)) return tt::invalid("trace_f32: t_end must be >= 0");
-    if (!(opts->rtol > 0.0) || !(opts->atol > 0.0))
-        return tt::invalid("trace_f32: need rtol > 0 and atol > 0 (cells)");
-    if (opts->with_phase && !(opts->atol_phase > 0.0)) return tt::invalid("trace_f32: need atol_phase > 0");
-    for (int i = 0; i < 3; ++i)
-        if (vol->n[i] < 2) return tt::invalid("trace_f32: volume axis with < 2 nodes");
+    GeoTable& H = host_table();
+    H.n = 1;
+    TT_TRY(make_geo(vol, t_end, extent, 0, np, 0, &H.g[0]));
+    Ctl K;
+    TT_TRY(make_ctl(opts, &K));
     if (np == 0) return TT_OK;
     if (!s0) return tt::invalid("trace_f32: s0 is null");
-    const WsLayout L = ws_layout(vol, np);
-    if (!workspace || workspace_bytes < L.total) {
-        tt::set_detail("trace_f32: workspace needs %zu bytes", L.total);
-        return TT_ERR_WORKSPACE_TOO_SMALL;
-    }
-    static const Tab T = make_tab();
-    Vol32 V;
-    V.nodes = static_cast<const float4*>(vol->nodes);
-    for (int i = 0; i < 3; ++i) {
-        V.n[i] = vol->n[i];
-        V.origin[i] = vol->origin[i];
-        V.spacing[i] = vol->spacing[i];
-        V.inv_spacing[i] = 1.0 / vol->spacing[i];
-        V.axis[i] = vol->axis[i];
-        V.r[i] = (float)(vol->spacing[2] / vol->spacing[i]);
-    }
-    V.st_b = vol->supertiles[1];
-    V.tile_f4 = (long long)vol->bricks_c * 200;
-    V.kappa = (float)(vol->omega / TT_C_LIGHT * vol->spacing[2]);
-    V.sig_end = t_end * TT_C_LIGHT / vol->spacing[2];
-    V.sig_end_f = (float)V.sig_end;
-    V.t_end = t_end;
-    V.extent = extent;
-    V.rtol = (float)opts->rtol;
-    V.atol_cells = (float)opts->atol;
-    V.inv_rtol = (float)(1.0 / opts->rtol);
-    V.inv_atol_cells = (float)(1.0 / opts->atol);
-    V.atol_phase = (float)(opts->with_phase ? opts->atol_phase : 1.0);
-    V.with_phase = opts->with_phase ? 1 : 0;
-    V.max_steps = opts->max_steps > 0 ? opts->max_steps : TT_DEFAULT_MAX_STEPS;
+    return run(H, vol_bins(vol), K, opts->block_size, s0, np, sf, rf, phase, status, nsteps, workspace,
+               workspace_bytes, tt::as_stream(stream), "trace_f32");
+}
 
-    cudaStream_t s = tt::as_stream(stream);
-    char* ws = static_cast<char*>(workspace);
-    unsigned long long* counter = reinterpret_cast<unsigned long long*>(ws + L.counter_off);
-    unsigned* cnt = reinterpret_cast<unsigned*>(ws + L.cnt_off);
-    unsigned* perm = reinterpret_cast<unsigned*>(ws + L.perm_off);
-    TT_TRY(tt::cuda_status(cudaMemsetAsync(ws, 0, L.perm_off, s), "trace_f32 workspace clear"));
-    long long g = (np + 255) / 256;
-    const long long cap = (long long)tt::sm_count() * 16;
-    if (g > cap) g = cap;
-    bin_count_kernel<<<(int)g, 256, 0, s>>>(V, s0, np, cnt);
-    bin_scan_kernel<<<1, 1024, 0, s>>>(cnt, L.nbins);
-    bin_scatter_kernel<<<(int)g, 256, 0, s>>>(V, s0, np, cnt, perm);
-    TT_TRY(tt::launch_status("trace_f32 ray binning"));
-    trace32_kernel<<<occupancy_grid(), 128, 0, s>>>(V, T, s0, np, perm, counter, sf, rf, phase, status, nsteps);
-    return tt::launch_status("trace_f32 kernel");
+extern "C" size_t tt_trace_f32_batched_workspace_bytes(const tt_volume* vols, int ninst, int64_t ntot)
+{
+    if (!vols || ninst < 1 || ninst > TT_MAX_INSTANCES || ntot < 0) return 0;
+    int nb = 0;
+    for (int i = 0; i < ninst; ++i) nb += vol_bins(&vols[i]);
+    return ws_layout(nb, ntot).total;
+}
+
+extern "C" int tt_trace_f32_batched(const tt_volume* vols, int ninst, const int64_t* ray_offsets,
+                                    const double* t_end, const double* extent, const double* s0,
+                                    const tt_trace_opts* opts, double* sf, double* rf, double* phase,
+                                    int32_t* status, int32_t* nsteps, void* workspace, size_t workspace_bytes,
+                                    void* stream)
+{
+    if (!vols || !opts || !ray_offsets || !t_end || !extent) return tt::invalid("trace_f32_batched: null argument");
+    if (ninst < 1 || ninst > TT_MAX_INSTANCES) return tt::invalid("trace_f32_batched: 1..TT_MAX_INSTANCES instances");
+    if (ray_offsets[0] != 0) return tt::invalid("trace_f32_batched: ray_offsets[0] must be 0");
+    for (int i = 0; i < ninst; ++i)
+        if (ray_offsets[i + 1] < ray_offsets[i]) return tt::invalid("trace_f32_batched: ray_offsets must not decrease");
+    const long long np = ray_offsets[ninst];
+    if (np > 0xffffffffLL) return tt::invalid("trace_f32_batched: at most 2^32-1 rays per call");
+    Ctl K;
+    TT_TRY(make_ctl(opts, &K));
+    GeoTable& H = host_table();
+    H.n = ninst;
+    int nb = 0;
+    for (int i = 0; i < ninst; ++i) {
+        TT_TRY(make_geo(&vols[i], t_end[i], extent[i], ray_offsets[i], ray_offsets[i + 1] - ray_offsets[i], nb,
+                        &H.g[i]));
+        nb += vol_bins(&vols[i]);
+    }
+    if (np == 0) return TT_OK;
+    if (!s0) return tt::invalid("trace_f32_batched: s0 is null");
+    // an empty instance owns no ray: instance_of() picks the last instance
+    // starting at or before a ray, which is never an empty one
+    return run(H, nb, K, opts->block_size, s0, np, sf, rf, phase, status, nsteps, workspace, workspace_bytes,
+               tt::as_stream(stream), "trace_f32_batched");
 }

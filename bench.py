@@ -36,6 +36,12 @@ import numpy as np  # noqa: E402
 METRIC = "ray-steps/s at 512^3, 1e7 rays (FP32 persistent tracer, phase on, <=1 urad vs FP64)"
 UNIT = "ray-steps/s"
 ALG_BYTES_PHASE = 768  # 6 stages x 8 corners x 4 components x 4 B per ray-step (phase needs ne_nc)
+# DRAM traffic of one trace32_kernel launch on the default workload, from one
+# one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum; the
+# command and figures are in profiles/trace32_grf512_1e7rays_dram.md).  Other
+# workloads scale it by accepted ray-steps, which is stated in the output.
+TRAFFIC_CAPTURE = {"workload": "grf512_1e+07rays_phase_3det1024", "read_bytes": 15.59e9, "write_bytes": 5.34e9,
+                   "ray_steps": 4225486610}
 
 
 def parse():
@@ -266,10 +272,15 @@ def run_ours(a):
     alg_bytes = ray_steps_step * ALG_BYTES_PHASE
     roof = {"kernel": "tt_trace_f32 (ray bucketing + persistent trace32_kernel)", "bound": "hbm",
             "achieved": alg_bytes / (trace_ms_avg / 1e3) / 1e9, "peak": peak, "peak_kind": peak_kind,
-            "unit": "GB/s", "traffic": None,
+            "unit": "GB/s", "traffic": traffic_per_launch(workload_config(a)["workload"], ray_steps_step),
+            "traffic_source": ("ncu capture of this workload"
+                               if workload_config(a)["workload"] == TRAFFIC_CAPTURE["workload"]
+                               else "ncu capture of %s scaled by ray-steps" % TRAFFIC_CAPTURE["workload"]),
             "note": "algorithmic bytes = 768 B per ray-step (6 stages x 8 corners x 4 comps x 4 B); "
-                    "a face-clamped step reads one cell's 8 nodes once, so frac > 1 is cache reuse"}
+                    "a face-clamped step reads one cell's 8 nodes once and rays bucketed by entry tile "
+                    "share them in L1/L2, so DRAM traffic is ~5 B per ray-step and frac > 1 is cache reuse"}
     roof["frac"] = roof["achieved"] / peak
+    roof["dram_gbs"] = roof["traffic"] / (trace_ms_avg / 1e3) / 1e9
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32", "data": "synthetic (seeded GRF density and Gaussian beam)",
@@ -292,6 +303,16 @@ def run_ours(a):
     if dist:
         dist.destroy_process_group()
     return res if rank == 0 else None
+
+
+def traffic_per_launch(workload, ray_steps):
+    """DRAM bytes per trace launch: the ncu capture's, scaled by accepted
+    ray-steps when the workload differs from the captured one."""
+    cap = TRAFFIC_CAPTURE
+    b = cap["read_bytes"] + cap["write_bytes"]
+    if workload == cap["workload"] and ray_steps == cap["ray_steps"]:
+        return b
+    return b * ray_steps / cap["ray_steps"]
 
 
 def fp64_compare(a, core, ne, x, s0_host, t_end, ext, out32, rays_per_s32):

@@ -250,6 +250,86 @@ int tt_grf_field(uint64_t seed, int n, double L, double alpha, double kmin, doub
  * out (4, count) uint32.  Exposed for known-answer tests of the generator. */
 int tt_philox(uint64_t seed, uint32_t tag, int64_t count, uint32_t* out, void* stream);
 
+/* Straight-line path integrals through an n_e grid along z, at the centres of
+ * a P x P pixel grid over the box face (pixel (i, j) at x0 + (i + 0.5)(xN - x0)/P,
+ * y0 + (j + 0.5)(yN - y0)/P): out FP32 [3][P][P] =
+ *   -1/2 integral dq/dx dz, -1/2 integral dq/dy dz (straight-line deflection, rad),
+ *   k0 integral (sqrt(1 - q) - 1) dz (straight-line phase, rad),
+ * q = min(ne / n_c, ne_max) with n_c and k0 = omega / c as calc_dndr forms them
+ * (particle_tracker.py:227-232), gradients by numpy.gradient's rule, all fields
+ * trilinear.  x, y, z: host arrays of uniform node coordinates. */
+int tt_straight_line_maps(const void* ne, int ne_dtype, int nx, int ny, int nz, const double* x, const double* y,
+                          const double* z, double lwl, double ne_max, int P, float* out, void* stream);
+
+/* ---- Learned surrogate: 2D Fourier neural operator ----------------------------
+ * No reference interface: the reference has no surrogate.  The network maps
+ * straight-line path-integrated gradient maps to the full-trace deflection and
+ * phase correction on the same S x S grid (S in {128, 256}): a pointwise lift
+ * of the in_ch data channels plus two coordinate channels (row, column, each
+ * (i + 0.5) 2/S - 1) to width 32, `layers` Fourier layers (truncated DFT
+ * keeping 16 x 32 modes, per-mode complex 32 x 32 mixing, inverse DFT, plus a
+ * 1x1 convolution and bias, then GELU), and a pointwise projection to out_ch.
+ * Activations are bfloat16 with FP32 accumulation; every contraction over
+ * pixels runs on the tcgen05 tensor cores.
+ *
+ * Parameters are one FP32 array, in this order (C = 32, M = 512 modes, cin = in_ch + 2):
+ *   P [C][cin], pb [C], then per layer: W [C][C], b [C], R [M][C][C][2] (complex
+ *   R[mode][out][in], mode = kyi * 16 + kx, kyi < 16: ky = kyi, else ky = S - 32 + kyi),
+ *   then Q [out_ch][C], qb [out_ch].
+ * Inputs a: FP32 [batch][in_ch][S][S]; targets and outputs: FP32 [batch][out_ch][S][S]. */
+#define TT_FNO_WIDTH 32
+#define TT_FNO_MODES 16
+#define TT_FNO_MAX_LAYERS 8
+#define TT_FNO_MAX_IN 8
+#define TT_FNO_MAX_OUT 4
+
+typedef struct tt_fno_dims {
+    int32_t batch;
+    int32_t size;   /* S */
+    int32_t in_ch;  /* data channels, 1..TT_FNO_MAX_IN */
+    int32_t out_ch; /* 1..TT_FNO_MAX_OUT */
+    int32_t layers; /* 1..TT_FNO_MAX_LAYERS */
+} tt_fno_dims;
+
+size_t tt_fno_param_count(const tt_fno_dims* d);
+/* training != 0: room for the activations the backward pass needs. */
+size_t tt_fno_workspace_bytes(const tt_fno_dims* d, int training);
+
+/* Inference: out = network(a). */
+int tt_fno_forward(const tt_fno_dims* d, const float* params, const float* a, float* out, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/* One forward + backward pass: *loss (device) += sum_k w_k sum (out - target)^2 / (batch S^2)
+ * and grads (same layout as params) += its gradient.  channel_weights: host array of
+ * out_ch weights (NULL = all 1); out (optional) receives the prediction. */
+int tt_fno_train_step(const tt_fno_dims* d, const float* params, float* grads, const float* a, const float* target,
+                      const float* channel_weights, float* loss, float* out, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+/* Adam update of n parameters (bias-corrected, step counts from 1); zeroes grads. */
+int tt_fno_adam(int64_t n, float* params, float* grads, float* m, float* v, float lr, float beta1, float beta2,
+                float eps, int64_t step, void* stream);
+
+/* Device error flag in a workspace (1 after a bounded tensor-core wait ran out). Synchronous. */
+int tt_fno_error_flag(const void* workspace, int* host_flag);
+
+/* The tensor-core building blocks, for tests.  Operands "packed" are bf16
+ * matrices in the canonical K-major tcgen05 layout written by tt_fno_pack
+ * (rows % 8 == 0, k % 8 == 0).  workspace: >= 256 bytes, zeroed (error flag).
+ *   rowdft: out[r][j] = sum_x in[r][x] mat[j][x]; in bf16 [rows][S], rows % 128 == 0,
+ *           mat packed [32][S], out FP32 [rows][32].
+ *   mix:    acc[x][o] = sum_c in[b][c][y][x] w[o][c] + sum_j a[x][j] sp[b][o][y][j] over every
+ *           (b, y, x); w packed [32][32], a packed [S][32], sp FP32 [B][32][S][32].
+ *           mode 0: out0 = bf16(acc + bias) (if out0), out1 = bf16(GELU(out0));
+ *           mode 1: out0 = bf16(acc * GELU'(zprev)) (zprev NULL: acc).  Outputs bf16 [B][32][S][S].
+ *   wgrad:  dW[o][c] += sum_{b,p} dz[b][o][p] v[b][c][p], db[o] += sum dz[b][o][p]; dz, v bf16 [B][32][S*S]. */
+int tt_fno_pack(int64_t rows, int k, const float* src, void* dst, void* stream);
+int tt_fno_rowdft(int S, int64_t rows, const void* in, const void* mat_packed, float* out, void* workspace,
+                  void* stream);
+int tt_fno_mix(int S, int B, int mode, const void* in, const void* w_packed, const void* a_packed, const float* sp,
+               const float* bias, const void* zprev, void* out0, void* out1, void* workspace, void* stream);
+int tt_fno_wgrad(int S, int B, const void* dz, const void* v, float* dW, float* db, void* workspace, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

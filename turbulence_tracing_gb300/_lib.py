@@ -56,6 +56,18 @@ class TTTraceOpts(ctypes.Structure):
                 ("max_steps", ctypes.c_int64), ("with_phase", ctypes.c_int32), ("block_size", ctypes.c_int32)]
 
 
+class TTFnoDims(ctypes.Structure):
+    _fields_ = [("batch", ctypes.c_int32), ("size", ctypes.c_int32), ("in_ch", ctypes.c_int32),
+                ("out_ch", ctypes.c_int32), ("layers", ctypes.c_int32)]
+
+
+FNO_WIDTH = 32
+FNO_MODES = 16
+FNO_MAX_LAYERS = 8
+FNO_MAX_IN = 8
+FNO_MAX_OUT = 4
+
+
 class TTOptic(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("reserved", ctypes.c_int32), ("p", ctypes.c_double * 3)]
 
@@ -101,6 +113,21 @@ SIGNATURES = {
                              ctypes.c_double, ctypes.c_double, ctypes.c_double, c_int, c_void_p, c_void_p,
                              c_size, c_void_p]),
     "tt_philox": (c_int, [ctypes.c_uint64, ctypes.c_uint32, c_i64, c_void_p, c_void_p]),
+    "tt_straight_line_maps": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_double_p, c_double_p, c_double_p,
+                                      ctypes.c_double, ctypes.c_double, c_int, c_void_p, c_void_p]),
+    "tt_fno_param_count": (c_size, [ctypes.POINTER(TTFnoDims)]),
+    "tt_fno_workspace_bytes": (c_size, [ctypes.POINTER(TTFnoDims), c_int]),
+    "tt_fno_forward": (c_int, [ctypes.POINTER(TTFnoDims), c_void_p, c_void_p, c_void_p, c_void_p, c_size, c_void_p]),
+    "tt_fno_train_step": (c_int, [ctypes.POINTER(TTFnoDims), c_void_p, c_void_p, c_void_p, c_void_p,
+                                  ctypes.POINTER(ctypes.c_float), c_void_p, c_void_p, c_void_p, c_size, c_void_p]),
+    "tt_fno_adam": (c_int, [c_i64, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_float, ctypes.c_float,
+                            ctypes.c_float, ctypes.c_float, c_i64, c_void_p]),
+    "tt_fno_error_flag": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
+    "tt_fno_pack": (c_int, [c_i64, c_int, c_void_p, c_void_p, c_void_p]),
+    "tt_fno_rowdft": (c_int, [c_int, c_i64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tt_fno_mix": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                           c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tt_fno_wgrad": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 _lib = None

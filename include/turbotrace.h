@@ -252,14 +252,22 @@ int tt_philox(uint64_t seed, uint32_t tag, int64_t count, uint32_t* out, void* s
 
 /* Straight-line path integrals through an n_e grid along z, at the centres of
  * a P x P pixel grid over the box face (pixel (i, j) at x0 + (i + 0.5)(xN - x0)/P,
- * y0 + (j + 0.5)(yN - y0)/P): out FP32 [3][P][P] =
+ * y0 + (j + 0.5)(yN - y0)/P): out FP32 [nout][P][P], nout 3 or 5 =
  *   -1/2 integral dq/dx dz, -1/2 integral dq/dy dz (straight-line deflection, rad),
  *   k0 integral (sqrt(1 - q) - 1) dz (straight-line phase, rad),
+ *   and with nout = 5 the first moments -1/2 integral (z - z0)/Lz dq/dx dz and the same for y,
  * q = min(ne / n_c, ne_max) with n_c and k0 = omega / c as calc_dndr forms them
  * (particle_tracker.py:227-232), gradients by numpy.gradient's rule, all fields
  * trilinear.  x, y, z: host arrays of uniform node coordinates. */
 int tt_straight_line_maps(const void* ne, int ne_dtype, int nx, int ny, int nz, const double* x, const double* y,
-                          const double* z, double lwl, double ne_max, int P, float* out, void* stream);
+                          const double* z, double lwl, double ne_max, int P, int nout, float* out, void* stream);
+
+/* Geometric-optics shadowgram of a deflection map theta FP32 [2][P][P] (angles
+ * of rays leaving the centres of a P x P pixel grid of pitch `pitch` m):
+ * intensity [P][P] = 1 / max(|det(I + D grad theta)|, 1e-3) after a free drift
+ * of D m, and div [P][P] = d theta_x/dx + d theta_y/dy (either output may be
+ * NULL); differences central inside, one-sided at the edges. */
+int tt_shadowgram(const float* theta, int P, double pitch, double D, float* intensity, float* div, void* stream);
 
 /* ---- Learned surrogate: 2D Fourier neural operator ----------------------------
  * No reference interface: the reference has no surrogate.  The network maps
@@ -309,6 +317,11 @@ int tt_fno_train_step(const tt_fno_dims* d, const float* params, float* grads, c
 /* Adam update of n parameters (bias-corrected, step counts from 1); zeroes grads. */
 int tt_fno_adam(int64_t n, float* params, float* grads, float* m, float* v, float lr, float beta1, float beta2,
                 float eps, int64_t step, void* stream);
+
+/* The same with the learning rate (*lr) and step counter (*step, incremented
+ * first) in device memory, for training steps captured in a CUDA graph. */
+int tt_fno_adam_device(int64_t n, float* params, float* grads, float* m, float* v, const float* lr, float beta1,
+                       float beta2, float eps, int64_t* step, void* stream);
 
 /* Device error flag in a workspace (1 after a bounded tensor-core wait ran out). Synchronous. */
 int tt_fno_error_flag(const void* workspace, int* host_flag);

@@ -16,15 +16,17 @@ pytestmark = pytest.mark.gpu
 def _small_ensemble(**kw):
     from turbulence_tracing_gb300 import ensemble
 
-    inst = ensemble.draw_instances(n_inst=6, seed=3, sizes=(24, 32, 40), rays=(200, 3000))
+    inst = ensemble.draw_instances(n_inst=7, seed=3, sizes=(24, 32, 40), rays=(200, 3000))
     inst[2]["nrays"] = 0  # an instance with no rays
     return ensemble.Ensemble(inst, L=1e-3, det=64, phase=True, **kw).setup()
 
 
-def test_batched_equals_single_launches(cuda):
+@pytest.mark.parametrize("grouped", [True, False])
+def test_batched_equals_single_launches(cuda, grouped):
+    """grouped: one uniform-shape launch per grid size; else one mixed-shape launch."""
     from turbulence_tracing_gb300 import core
 
-    E = _small_ensemble(tune=False)
+    E = _small_ensemble(tune=False, grouped=grouped)
     torch.cuda.synchronize()
     rf_b = E.out["rf"].clone()
     ph_b = E.out["phase"].clone()

@@ -1,0 +1,86 @@
+"""The learned surrogate end to end at 128^2: straight-line maps against a
+direct restatement, the exact tracer as the judge of held-out fields, and
+what the trained network gains over the straight-line method without it."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import restated as R
+
+pytestmark = pytest.mark.gpu
+
+
+def _maps_restated(ne, x, lwl, S):
+    """Straight-line deflection maps in float64: numpy.gradient of q = ne/n_c,
+    bilinear at pixel centres, trapezoid along z."""
+    omega, nc = R.critical_density(lwl)
+    q = np.minimum(ne / nc, 1.0)
+    h = x[1] - x[0]
+    gx, gy = np.gradient(q, h, axis=0), np.gradient(q, h, axis=1)
+    pc = (np.arange(S) + 0.5) / S * (len(x) - 1)
+    i0 = np.clip(np.floor(pc).astype(int), 0, len(x) - 2)
+    f = pc - i0
+
+    def bil(F):
+        A, B, C, D = F[i0][:, i0], F[i0 + 1][:, i0], F[i0][:, i0 + 1], F[i0 + 1][:, i0 + 1]
+        fx, fy = f[:, None, None], f[None, :, None]
+        return (1 - fx) * (1 - fy) * A + fx * (1 - fy) * B + (1 - fx) * fy * C + fx * fy * D
+
+    w = np.full(len(x), h)
+    w[0] = w[-1] = h / 2
+    return -0.5 * (bil(gx) * w).sum(-1), -0.5 * (bil(gy) * w).sum(-1)
+
+
+def test_straight_line_maps_match_restatement(cuda):
+    from turbulence_tracing_gb300 import core
+
+    ne, x = R.workload_density(40, 1e-3, -3.0, 0.2, 5e24, 3)
+    m = core.straight_line_maps(ne, x, x, x, 32, lwl=1064e-9, moments=True).cpu().numpy()
+    ax, ay = _maps_restated(ne, x, 1064e-9, 32)
+    scale = np.abs(ax).max()
+    assert np.abs(m[0] - ax).max() <= 1e-5 * scale
+    assert np.abs(m[1] - ay).max() <= 1e-5 * scale
+
+
+def test_straight_line_map_is_first_order_trace(cuda):
+    """The straight-line map is the first-order term of the exact trace: the
+    difference is second order in the field, so relative to the deflection it
+    halves when the fluctuation amplitude halves."""
+    from turbulence_tracing_gb300 import surrogate as SG
+
+    W = SG.Workload(128)
+    errs = []
+    for delta in (0.2, 0.1):
+        ne = W.field(dict(alpha=-11 / 3, delta=delta, ne0=2e24, seed=5))
+        m = W.maps(ne)
+        theta, _, _ = W.trace(ne)
+        errs.append(SG.rel_l2(m[0:2], theta))
+    assert errs[0] < 0.1, errs
+    assert 1.5 < errs[0] / errs[1] < 2.7, errs
+
+
+def test_trained_surrogate_beats_straight_line_and_fallback_bounds_error(cuda):
+    from turbulence_tracing_gb300 import fno, surrogate as SG
+
+    W = SG.Workload(128)
+    Xtr, Ytr, _, _, _ = SG.build_dataset(W, SG.draw_fields(384, seed=1))
+    Xte, _, ste, truth, _ = SG.build_dataset(W, SG.draw_fields(48, seed=2), keep_truth=True)
+    net = fno.FNO(128, in_ch=SG.IN_CH, out_ch=3, layers=4, seed=0)
+    hist, _ = SG.Trainer(net, Xtr, Ytr, batch=8).fit(12, lr=1e-3)
+    assert hist[-1] < 0.7 * hist[0], hist
+    res = SG.evaluate(W, net, Xte, ste, truth)
+    assert net.error_flag() == 0
+    e_s = np.array([r["err_straight"] for r in res])
+    e_n = np.array([r["err_net"] for r in res])
+    ph = np.array([r["phase_corr_err_net"] for r in res])
+    strong = e_s > 0.02
+    # the network's shadowgrams are closer to the exact trace than the straight-line ones
+    assert e_n[strong].mean() < 0.95 * e_s[strong].mean(), (e_n[strong].mean(), e_s[strong].mean())
+    # and it recovers part of the phase correction the straight-line method misses entirely
+    assert np.median(ph) < 1.0, np.median(ph)
+    # fallback: fields whose estimate exceeds the tolerance are traced; the accepted
+    # ones stay within tolerance for the calibrated quantile
+    kappa = SG.calibrate(res[:24])
+    est = np.array([kappa * r["moved"] for r in res[24:]])
+    acc = est <= 0.02
+    assert np.all(e_n[24:][acc] <= 0.03), e_n[24:][acc]

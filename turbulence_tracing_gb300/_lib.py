@@ -114,7 +114,8 @@ SIGNATURES = {
                              c_size, c_void_p]),
     "tt_philox": (c_int, [ctypes.c_uint64, ctypes.c_uint32, c_i64, c_void_p, c_void_p]),
     "tt_straight_line_maps": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_double_p, c_double_p, c_double_p,
-                                      ctypes.c_double, ctypes.c_double, c_int, c_void_p, c_void_p]),
+                                      ctypes.c_double, ctypes.c_double, c_int, c_int, c_void_p, c_void_p]),
+    "tt_shadowgram": (c_int, [c_void_p, c_int, ctypes.c_double, ctypes.c_double, c_void_p, c_void_p, c_void_p]),
     "tt_fno_param_count": (c_size, [ctypes.POINTER(TTFnoDims)]),
     "tt_fno_workspace_bytes": (c_size, [ctypes.POINTER(TTFnoDims), c_int]),
     "tt_fno_forward": (c_int, [ctypes.POINTER(TTFnoDims), c_void_p, c_void_p, c_void_p, c_void_p, c_size, c_void_p]),
@@ -122,6 +123,8 @@ SIGNATURES = {
                                   ctypes.POINTER(ctypes.c_float), c_void_p, c_void_p, c_void_p, c_size, c_void_p]),
     "tt_fno_adam": (c_int, [c_i64, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_float, ctypes.c_float,
                             ctypes.c_float, ctypes.c_float, c_i64, c_void_p]),
+    "tt_fno_adam_device": (c_int, [c_i64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_float,
+                                   ctypes.c_float, ctypes.c_float, c_void_p, c_void_p]),
     "tt_fno_error_flag": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
     "tt_fno_pack": (c_int, [c_i64, c_int, c_void_p, c_void_p, c_void_p]),
     "tt_fno_rowdft": (c_int, [c_int, c_i64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -309,20 +309,37 @@ def detect(rf, ops, nbx=1, nby=1, xr=(-1.0, 1.0), yr=(-1.0, 1.0), weights=None, 
 # ---------------------------------------------------------------------------
 # K4
 # ---------------------------------------------------------------------------
-def straight_line_maps(ne, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None):
+def straight_line_maps(ne, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, moments=False):
     """(3, P, P) float32: straight-line deflection angles (x, y) and phase at
-    the centres of a P x P pixel grid over the z = z0 face (tt_straight_line_maps)."""
+    the centres of a P x P pixel grid over the z = z0 face (tt_straight_line_maps);
+    with moments=True (5, P, P), adding the first z-moments of the deflection."""
     dev = require_cuda()
     ne_t = _dens_dev(ne, dev)
     nx, ny, nz = ne_t.shape
     xa, ya, za = (np.ascontiguousarray(np.asarray(c, dtype=np.float64)) for c in (x, y, z))
+    nout = 5 if moments else 3
     if out is None:
-        out = torch.empty((3, P, P), dtype=torch.float32, device=dev)
+        out = torch.empty((nout, P, P), dtype=torch.float32, device=dev)
     dp = ctypes.POINTER(ctypes.c_double)
     check(_lib.lib().tt_straight_line_maps(_ptr(ne_t), _dtype_code(ne_t), nx, ny, nz, xa.ctypes.data_as(dp),
                                            ya.ctypes.data_as(dp), za.ctypes.data_as(dp), float(lwl), float(ne_max),
-                                           int(P), _ptr(out), _stream()), "tt_straight_line_maps")
+                                           int(P), nout, _ptr(out), _stream()), "tt_straight_line_maps")
     return out
+
+
+def shadowgram(theta, pitch, D, intensity=None, div=None, want_intensity=True, want_div=False):
+    """Geometric-optics shadowgram of a (2, P, P) float32 deflection map (tt_shadowgram).
+    Returns (intensity, div); either is None when not asked for."""
+    dev = require_cuda()
+    P = theta.shape[-1]
+    if want_intensity and intensity is None:
+        intensity = torch.empty((P, P), dtype=torch.float32, device=dev)
+    if want_div and div is None:
+        div = torch.empty((P, P), dtype=torch.float32, device=dev)
+    check(_lib.lib().tt_shadowgram(_ptr(theta), P, float(pitch), float(D),
+                                   _ptr(intensity) if want_intensity else None,
+                                   _ptr(div) if want_div else None, _stream()), "tt_shadowgram")
+    return (intensity if want_intensity else None), (div if want_div else None)
 
 
 def grf_field(n, L_box, alpha, ne0, delta, seed, dtype=torch.float32, kmin=None, kmax=None):

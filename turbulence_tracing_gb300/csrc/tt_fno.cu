@@ -787,6 +787,34 @@ __global__ void fno_adam_kernel(long long n, float* __restrict__ p, float* __res
     }
 }
 
+// The same update with the learning rate and the step counter in device
+// memory, so a captured training step can be replayed with a schedule.
+__global__ void fno_step_inc_kernel(long long* step) { *step += 1; }
+
+__global__ void fno_adam_dev_kernel(long long n, float* __restrict__ p, float* __restrict__ g, float* __restrict__ m,
+                                    float* __restrict__ v, const float* __restrict__ lr_dev, float b1, float b2,
+                                    float eps, const long long* __restrict__ step)
+{
+    __shared__ float sc[3];
+    if (threadIdx.x == 0) {
+        const float t = (float)*step;
+        sc[0] = *lr_dev;
+        sc[1] = 1.0f - powf(b1, t);
+        sc[2] = 1.0f - powf(b2, t);
+    }
+    __syncthreads();
+    const float lr = sc[0], bc1 = sc[1], bc2 = sc[2];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = fmaf(b1, m[i], (1.f - b1) * gi);
+        const float vi = fmaf(b2, v[i], (1.f - b2) * gi * gi);
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+        g[i] = 0.f;
+    }
+}
+
 // ----------------------------------------------------------------------------- host side
 int check_dims(const tt_fno_dims* d)
 {
@@ -1059,6 +1087,18 @@ int tt_fno_adam(int64_t n, float* params, float* grads, float* m, float* v, floa
     fno_adam_kernel<<<grid_for(n / 256 + 1, 4), 256, 0, tt::as_stream(stream)>>>(n, params, grads, m, v, lr, beta1,
                                                                                  beta2, eps, bc1, bc2);
     return tt::launch_status("fno_adam_kernel");
+}
+
+int tt_fno_adam_device(int64_t n, float* params, float* grads, float* m, float* v, const float* lr, float beta1,
+                       float beta2, float eps, int64_t* step, void* stream)
+{
+    if (n <= 0 || !params || !grads || !m || !v || !lr || !step) return tt::invalid("tt_fno_adam_device: bad arguments");
+    cudaStream_t st = tt::as_stream(stream);
+    fno_step_inc_kernel<<<1, 1, 0, st>>>(reinterpret_cast<long long*>(step));
+    TT_TRY(tt::launch_status("fno_step_inc_kernel"));
+    fno_adam_dev_kernel<<<grid_for(n / 256 + 1, 4), 256, 0, st>>>(n, params, grads, m, v, lr, beta1, beta2, eps,
+                                                                 reinterpret_cast<const long long*>(step));
+    return tt::launch_status("fno_adam_dev_kernel");
 }
 
 int tt_fno_error_flag(const void* ws, int* host_flag)

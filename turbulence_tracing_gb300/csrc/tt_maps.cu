@@ -7,6 +7,8 @@
 //   out[0] = -1/2 * integral dq/dx dz      (paraxial deflection angle, rad)
 //   out[1] = -1/2 * integral dq/dy dz
 //   out[2] = k0 * integral (sqrt(1 - q) - 1) dz   (phase, rad; k0 = omega / c)
+//   out[3] = -1/2 * integral (z - z0) / Lz dq/dx dz  (first moments along the path:
+//   out[4] = -1/2 * integral (z - z0) / Lz dq/dy dz   where along z the deflection builds up)
 // with q = min(ne / n_c, ne_max) and its gradient taken with numpy.gradient's
 // rule on the node grid (central inside, one-sided at the faces), both
 // interpolated trilinearly -- the same fields the tracer integrates.  The
@@ -35,7 +37,7 @@ __device__ __forceinline__ float grad1(F f, int i, int n)
 
 template <typename T>
 __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, double x0, double hx, double y0,
-                            double hy, double hz, float inv_nc, float ne_max, double k0, int P,
+                            double hy, double hz, float inv_nc, float ne_max, double k0, int P, int nout,
                             float* __restrict__ out)
 {
     const int n = P * P;
@@ -49,7 +51,7 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
     iy = iy < 0 ? 0 : (iy > ny - 2 ? ny - 2 : iy);
     const float fx = (float)(xs / hx - ix), fy = (float)(ys / hy - iy);
     const float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w01 = (1.f - fx) * fy, w11 = fx * fy;
-    double sx = 0.0, sy = 0.0, sp = 0.0;
+    double sx = 0.0, sy = 0.0, sp = 0.0, mx = 0.0, my = 0.0;
     float qprev = 0.f;
     const float gw[4] = {0.0694318442029737f, 0.3300094782075719f, 0.6699905217924281f, 0.9305681557970263f};
     const float gwt[4] = {0.1739274225687269f, 0.3260725774312731f, 0.3260725774312731f, 0.1739274225687269f};
@@ -69,6 +71,10 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
         const double wz = (k == 0 || k == nz - 1) ? 0.5 : 1.0;
         sx += wz * gxk;
         sy += wz * gyk;
+        // first moment, trapezoid rule on the nodes
+        const double zr = (double)k / (double)(nz - 1);
+        mx += wz * zr * gxk;
+        my += wz * zr * gyk;
         if (k > 0) {
             float cell = 0.f;
 #pragma unroll
@@ -84,14 +90,19 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
     out[pix] = (float)(-0.5 * sx * hz / hx);
     out[n + pix] = (float)(-0.5 * sy * hz / hy);
     out[2 * n + pix] = (float)(k0 * sp * hz);
+    if (nout > 3) {
+        out[3 * n + pix] = (float)(-0.5 * mx * hz / hx);
+        out[4 * n + pix] = (float)(-0.5 * my * hz / hy);
+    }
 }
 
 }  // namespace
 
 extern "C" int tt_straight_line_maps(const void* ne, int ne_dtype, int nx, int ny, int nz, const double* x,
-                                     const double* y, const double* z, double lwl, double ne_max, int P, float* out,
-                                     void* stream)
+                                     const double* y, const double* z, double lwl, double ne_max, int P, int nout,
+                                     float* out, void* stream)
 {
+    if (nout != 3 && nout != 5) return tt::invalid("straight_line_maps: nout must be 3 or 5");
     if (!ne || !x || !y || !z || !out) return tt::invalid("straight_line_maps: NULL pointer");
     if (nx < 2 || ny < 2 || nz < 2 || P < 1) return tt::invalid("straight_line_maps: bad sizes");
     if (ne_dtype != TT_F32 && ne_dtype != TT_F64) return tt::invalid("straight_line_maps: ne_dtype");
@@ -106,9 +117,61 @@ extern "C" int tt_straight_line_maps(const void* ne, int ne_dtype, int nx, int n
     cudaStream_t s = tt::as_stream(stream);
     if (ne_dtype == TT_F32)
         maps_kernel<float><<<grid, 128, 0, s>>>((const float*)ne, nx, ny, nz, x[0], hx, y[0], hy, hz,
-                                                (float)(1.0 / nc), (float)ne_max, k0, P, out);
+                                                (float)(1.0 / nc), (float)ne_max, k0, P, nout, out);
     else
         maps_kernel<double><<<grid, 128, 0, s>>>((const double*)ne, nx, ny, nz, x[0], hx, y[0], hy, hz,
-                                                 (float)(1.0 / nc), (float)ne_max, k0, P, out);
+                                                 (float)(1.0 / nc), (float)ne_max, k0, P, nout, out);
     return tt::launch_status("straight_line_maps");
+}
+
+// Geometric-optics shadowgram of a deflection map: rays leaving pixel centres
+// of a P x P grid (pitch h) with angles theta = (tx, ty) land D further on at
+// x + D theta; the intensity relative to the uniform beam is 1 / |det J| with
+// J = I + D grad(theta) (central differences inside, one-sided at the edges),
+// floored at |det J| >= 1e-3 near caustics.  div = dtx/dx + dty/dy.
+namespace {
+
+__device__ __forceinline__ float dmap(const float* __restrict__ f, int i, int j, int P, int axis)
+{
+    if (axis == 0) {
+        if (i == 0) return f[P + j] - f[j];
+        if (i == P - 1) return f[(size_t)(P - 1) * P + j] - f[(size_t)(P - 2) * P + j];
+        return 0.5f * (f[(size_t)(i + 1) * P + j] - f[(size_t)(i - 1) * P + j]);
+    }
+    const float* r = f + (size_t)i * P;
+    if (j == 0) return r[1] - r[0];
+    if (j == P - 1) return r[P - 1] - r[P - 2];
+    return 0.5f * (r[j + 1] - r[j - 1]);
+}
+
+__global__ void shadow_kernel(const float* __restrict__ theta, int P, float inv_h, float D, float* __restrict__ I,
+                              float* __restrict__ div)
+{
+    const int n = P * P;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int i = p / P, j = p % P;
+    const float* tx = theta;
+    const float* ty = theta + n;
+    const float axx = dmap(tx, i, j, P, 0) * inv_h, axy = dmap(tx, i, j, P, 1) * inv_h;
+    const float ayx = dmap(ty, i, j, P, 0) * inv_h, ayy = dmap(ty, i, j, P, 1) * inv_h;
+    if (div) div[p] = axx + ayy;
+    if (I) {
+        const float det = (1.f + D * axx) * (1.f + D * ayy) - D * D * axy * ayx;
+        const float a = fabsf(det);
+        I[p] = 1.f / (a > 1e-3f ? a : 1e-3f);
+    }
+}
+
+}  // namespace
+
+extern "C" int tt_shadowgram(const float* theta, int P, double pitch, double D, float* intensity, float* div,
+                             void* stream)
+{
+    if (!theta || P < 2 || !(pitch > 0)) return tt::invalid("shadowgram: bad arguments");
+    if (!intensity && !div) return TT_OK;
+    const int n = P * P;
+    shadow_kernel<<<(n + 255) / 256, 256, 0, tt::as_stream(stream)>>>(theta, P, (float)(1.0 / pitch), (float)D,
+                                                                       intensity, div);
+    return tt::launch_status("shadowgram");
 }

@@ -23,8 +23,9 @@
 // resident blocks pulls them through one global work counter; each warp
 // refills its finished lanes with one warp-aggregated atomic (ballot / popc),
 // so lanes stay busy while rays with long and short paths mix.  In the batched
-// form each lane carries its ray's instance and reads that instance's
-// geometry from a shared-memory copy of the instance table.
+// forms each lane finds its ray's instance once per ray: volumes of one shape
+// share the single-volume kernel's constant geometry and differ only in node
+// buffer and ray block; volumes of mixed shapes read per-lane geometry.
 #include <math.h>
 #include <stddef.h>
 
@@ -159,12 +160,13 @@ __device__ __forceinline__ void poly(float v000, float v001, float v010, float v
     c[7] = ((v111 - v110) - (v101 - v100)) - ((v011 - v010) - (v001 - v000));
 }
 
-__device__ __forceinline__ void load_cell(const Geo& G, long long tbase, int ca, int cb, int cc, float (*coef)[8])
+__device__ __forceinline__ void load_cell(const Geo& G, const float4* __restrict__ nodes, long long tbase, int ca,
+                                          int cb, int cc, float (*coef)[8])
 {
     const int cl = cc & (G.bd - 1);
     const int dc = (cl == G.bd - 1) ? G.brick_f4 - (G.bd - 1) : 1;
     const long long base = tbase + (long long)(cc >> G.bd_shift) * G.brick_f4 + ((ca & 3) * 5 + (cb & 3)) * G.bd + cl;
-    const float4* p = G.nodes + base;
+    const float4* p = nodes + base;
     const int db = G.bd, da = 5 * G.bd;
     const float4 n000 = __ldg(p), n001 = __ldg(p + dc);
     const float4 n010 = __ldg(p + db), n011 = __ldg(p + db + dc);
@@ -314,12 +316,18 @@ __device__ __forceinline__ bool renormalise(const Geo& G, Ray& R)
 
 // Initialise from s0 (SI units, physical axes).  Returns false when the ray
 // never enters the box before t_end (straight line throughout).
-__device__ __forceinline__ bool init_ray(const Geo& G, const double* __restrict__ s0, long long np, long long r,
-                                         Ray& R, double P[3], double uu[3])
+// The rays of one volume: node buffer and its block of the instance-blocked arrays.
+struct Src {
+    const float4* nodes;
+    long long begin, count;
+};
+
+__device__ __forceinline__ bool init_ray(const Geo& G, const Src& src, const double* __restrict__ s0, long long np,
+                                         long long r, Ray& R, double P[3], double uu[3])
 {
     // instance-blocked arrays: this instance's s0 is (6, nrays) at 6 * ray_begin
-    const double* s = s0 + 6 * G.ray_begin;
-    const long long lr = r - G.ray_begin, ln = G.nrays;
+    const double* s = s0 + 6 * src.begin;
+    const long long lr = r - src.begin, ln = src.count;
     double x[3], v[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -398,8 +406,8 @@ __device__ __forceinline__ bool init_ray(const Geo& G, const double* __restrict_
     return true;
 }
 
-__device__ __forceinline__ void finish_ray(const Geo& G, const Ray& R, const double P0[3], const double u0[3],
-                                           long long r, long long np, double* __restrict__ sf,
+__device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const Ray& R, const double P0[3],
+                                           const double u0[3], long long r, long long np, double* __restrict__ sf,
                                            double* __restrict__ rf, double* __restrict__ phase,
                                            int* __restrict__ status, int* __restrict__ nsteps)
 {
@@ -431,14 +439,14 @@ __device__ __forceinline__ void finish_ray(const Geo& G, const Ray& R, const dou
         y[G.axis[a]] = G.origin[a] + P[a] * G.spacing[a];
         y[3 + G.axis[a]] = u[a] * TT_C_LIGHT;
     }
-    const long long lr = r - G.ray_begin, ln = G.nrays;
+    const long long lr = r - src.begin, ln = src.count;
     if (sf) {
-        double* o = sf + 6 * G.ray_begin;
+        double* o = sf + 6 * src.begin;
 #pragma unroll
         for (int i = 0; i < 6; ++i) o[(size_t)i * ln + lr] = y[i];
     }
     if (rf) {
-        double* o = rf + 4 * G.ray_begin;
+        double* o = rf + 4 * src.begin;
         const int ax = G.axis[2];
         const int p0 = ax == 0 ? 1 : 0, p1 = ax == 2 ? 1 : 2;
         const double tbp = (y[ax] - G.extent) / y[3 + ax];
@@ -457,8 +465,8 @@ __device__ __forceinline__ void finish_ray(const Geo& G, const Ray& R, const dou
 // Right-hand side at stage position Ps (fractions in the current cell):
 // the current cell's polynomial while Ps stays within kTolE of it (never past
 // a box face), the exact lookup otherwise.
-__device__ __forceinline__ void stage_eval(const Geo& G, const Ctl& K, const Ray& R, const float (*coef)[8],
-                                           const float Ps[3], float H[3], float& q)
+__device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, const Ray& R,
+                                           const float (*coef)[8], const float Ps[3], float H[3], float& q)
 {
     bool home = true;
 #pragma unroll
@@ -473,7 +481,7 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const Ctl& K, const Ray
         H[2] = tri(coef[2], Ps[0], Ps[1], Ps[2]);
         q = K.with_phase ? tri(coef[3], Ps[0], Ps[1], Ps[2]) : 0.f;
     } else {
-        const float4 r = eval_exact(G.nodes, G.n[0], G.n[1], G.n[2], G.st_b, G.tile_f4, G.bd, G.bd_shift,
+        const float4 r = eval_exact(nodes, G.n[0], G.n[1], G.n[2], G.st_b, G.tile_f4, G.bd, G.bd_shift,
                                     G.brick_f4, R.ci[0], R.ci[1], R.ci[2], Ps[0], Ps[1], Ps[2]);
         H[0] = r.x;
         H[1] = r.y;
@@ -483,7 +491,8 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const Ctl& K, const Ray
 }
 
 // One attempted step.  Returns with R updated.
-__device__ __forceinline__ void step(const Geo& G, const Ctl& K, const Tab& T, Ray& R, float (*coef)[8])
+__device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, const Tab& T, Ray& R,
+                                     float (*coef)[8])
 {
     if (R.cell_dirty) {
         const int ta = R.ci[0] >> 2, tb = R.ci[1] >> 2;
@@ -492,7 +501,7 @@ __device__ __forceinline__ void step(const Geo& G, const Ctl& K, const Tab& T, R
             R.tb = tb;
             R.tbase = tile_base(G, ta, tb);
         }
-        load_cell(G, R.tbase, R.ci[0], R.ci[1], R.ci[2], coef);
+        load_cell(G, nodes, R.tbase, R.ci[0], R.ci[1], R.ci[2], coef);
         R.cell_dirty = false;
     }
     const float rem = (G.sig_end_f - R.sig) - R.sigc;
@@ -507,7 +516,7 @@ __device__ __forceinline__ void step(const Geo& G, const Ctl& K, const Tab& T, R
     }
     float Hs[7][3];
     float q0;
-    stage_eval(G, K, R, coef, R.fr, Hs[0], q0);
+    stage_eval(G, nodes, K, R, coef, R.fr, Hs[0], q0);
     // Predict the first face crossing of the cell from position, velocity and
     // acceleration; aim the step end at it.  Leaving through a box face within
     // kBoxPath: the ray has left (the field beyond is the fill value 0).
@@ -558,7 +567,7 @@ __device__ __forceinline__ void step(const Geo& G, const Ctl& K, const Tab& T, R
             Ps[c] = fmaf(h * G.r[c], fmaf(T.cs[s], R.u[c], h * saa), R.fr[c]);
         }
         float q;
-        stage_eval(G, K, R, coef, Ps, Hs[s], q);
+        stage_eval(G, nodes, K, R, coef, Ps, Hs[s], q);
         if (K.with_phase) {
             const float u2 = fmaf(us[0], us[0], fmaf(us[1], us[1], us[2] * us[2]));
             const float sp = u2 * rsqrtf(u2);
@@ -678,8 +687,13 @@ __device__ __forceinline__ int instance_of(const Geo* g, int n, long long r)
 
 // The persistent loop, shared by the single-volume and batched kernels.
 // GeoOf(r) returns the geometry of ray r's instance.
-template <typename GeoOf>
-__device__ __forceinline__ void persistent_loop(GeoOf geo_of, const Ctl& K, const Tab& T, const double* __restrict__ s0,
+// The persistent loop, shared by the single-volume and batched kernels.  The
+// policy gives, for ray r: the geometry of its volume (geo), and its ray
+// block (src: node buffer and the block of the instance-blocked arrays).  It
+// is asked once per fetched ray; the node pointer is kept for the ray's steps
+// unless the policy has it as a constant (pol.nodes).
+template <typename Policy>
+__device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const Tab& T, const double* __restrict__ s0,
                                                 long long np, const unsigned* __restrict__ perm,
                                                 unsigned long long* __restrict__ counter, double* __restrict__ sf,
                                                 double* __restrict__ rf, double* __restrict__ phase,
@@ -689,6 +703,7 @@ __device__ __forceinline__ void persistent_loop(GeoOf geo_of, const Ctl& K, cons
     long long idx = -1;      // position in perm of this lane's ray
     long long ray = 0;
     bool drained = false;
+    const float4* nodes = nullptr;
     Ray R;
     double P0[3], u0[3];
     float coef[4][8];
@@ -706,8 +721,10 @@ __device__ __forceinline__ void persistent_loop(GeoOf geo_of, const Ctl& K, cons
                 if (my < (unsigned long long)np) {
                     idx = (long long)my;
                     ray = perm ? (long long)perm[idx] : idx;
-                    if (!init_ray(geo_of(ray), s0, np, ray, R, P0, u0)) {
-                        finish_ray(geo_of(ray), R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
+                    const Src src = pol.src(ray);
+                    nodes = src.nodes;
+                    if (!init_ray(pol.geo(ray), src, s0, np, ray, R, P0, u0)) {
+                        finish_ray(pol.geo(ray), src, R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
                         idx = -1;  // picked up again on the next pass
                     }
                 } else {
@@ -718,18 +735,20 @@ __device__ __forceinline__ void persistent_loop(GeoOf geo_of, const Ctl& K, cons
         const bool active = idx >= 0;
         if (__ballot_sync(0xffffffffu, active || (!drained)) == 0u) break;
         if (active) {
-            step(geo_of(ray), K, T, R, coef);
+            step(pol.geo(ray), pol.nodes(nodes), K, T, R, coef);
             if (R.state != 0) {
-                finish_ray(geo_of(ray), R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
+                finish_ray(pol.geo(ray), pol.src(ray), R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
                 idx = -1;
             }
         }
     }
 }
 
-struct SingleGeo {
+struct SinglePolicy {
     const Geo* g;
-    __device__ __forceinline__ const Geo& operator()(long long) const { return *g; }
+    __device__ __forceinline__ const Geo& geo(long long) const { return *g; }
+    __device__ __forceinline__ Src src(long long) const { return Src{g->nodes, g->ray_begin, g->nrays}; }
+    __device__ __forceinline__ const float4* nodes(const float4*) const { return g->nodes; }
 };
 
 template <int BLOCK>
@@ -739,8 +758,35 @@ trace32_kernel(const Geo G, Ctl K, Tab T, const double* __restrict__ s0, long lo
                double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
                int* __restrict__ status, int* __restrict__ nsteps)
 {
-    persistent_loop(SingleGeo{&G}, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps);
+    persistent_loop(SinglePolicy{&G}, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps);
 }
+
+// Volumes of different shapes: each lane reads its ray's instance entry from
+// the table, which stays in the parameter bank (__grid_constant__); the lane
+// keeps a pointer to the entry of its current ray.  (A shared-memory copy of
+// the table measured 3-8% slower.)
+struct MixedPolicy {
+    const Geo* g;
+    int n;
+    mutable long long last_ray;
+    mutable const Geo* cur;
+    __device__ __forceinline__ const Geo& geo(long long r) const
+    {
+        if (r != last_ray) {
+            // rays reach a lane in bucket order, which is instance-major, so the
+            // lane's previous instance nearly always owns the next ray too
+            if (r < cur->ray_begin || r - cur->ray_begin >= cur->nrays) cur = g + instance_of(g, n, r);
+            last_ray = r;
+        }
+        return *cur;
+    }
+    __device__ __forceinline__ Src src(long long r) const
+    {
+        const Geo& e = geo(r);
+        return Src{e.nodes, e.ray_begin, e.nrays};
+    }
+    __device__ __forceinline__ const float4* nodes(const float4* kept) const { return kept; }
+};
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK, 512 / BLOCK)
@@ -749,30 +795,35 @@ trace32_batched_kernel(const __grid_constant__ GeoTable table, Ctl K, Tab T, con
                        double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
                        int* __restrict__ status, int* __restrict__ nsteps)
 {
-    // The table stays in the parameter bank (__grid_constant__): a lane's
-    // instance is found once per fetched ray and the lane keeps a pointer to
-    // that entry, so field reads are constant-cache loads, broadcast within a
-    // warp whose lanes share an instance.  (Copying the table to shared memory
-    // first measured 3-8% slower.)
-    const Geo* sg = table.g;
-    const int ninst = table.n;
-    struct BatchGeo {
-        const Geo* sg;
-        int n;
-        mutable long long last_ray;
-        mutable const Geo* cur;
-        __device__ __forceinline__ const Geo& operator()(long long r) const
-        {
-            if (r != last_ray) {
-                // rays reach a lane in bucket order, which is instance-major, so the
-                // lane's previous instance nearly always owns the next ray too
-                if (r < cur->ray_begin || r - cur->ray_begin >= cur->nrays) cur = sg + instance_of(sg, n, r);
-                last_ray = r;
-            }
-            return *cur;
-        }
-    };
-    persistent_loop(BatchGeo{sg, ninst, -1, sg}, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps);
+    persistent_loop(MixedPolicy{table.g, table.n, -1, table.g}, K, T, s0, np, perm, counter, sf, rf, phase, status,
+                    nsteps);
+}
+
+// Volumes of one shape (grid, spacing, brick depth, t_end): the geometry is
+// the first entry, read from the constant bank like the single-volume kernel;
+// only the node buffer and the ray block differ per instance.
+struct UniformPolicy {
+    const Geo* g;
+    int n;
+    mutable const Geo* cur;
+    __device__ __forceinline__ const Geo& geo(long long) const { return g[0]; }
+    __device__ __forceinline__ Src src(long long r) const
+    {
+        if (r < cur->ray_begin || r - cur->ray_begin >= cur->nrays) cur = g + instance_of(g, n, r);
+        return Src{cur->nodes, cur->ray_begin, cur->nrays};
+    }
+    __device__ __forceinline__ const float4* nodes(const float4* kept) const { return kept; }
+};
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 512 / BLOCK)
+trace32_uniform_kernel(const __grid_constant__ GeoTable table, Ctl K, Tab T, const double* __restrict__ s0,
+                       long long np, const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
+                       double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
+                       int* __restrict__ status, int* __restrict__ nsteps)
+{
+    persistent_loop(UniformPolicy{table.g, table.n, table.g}, K, T, s0, np, perm, counter, sf, rf, phase, status,
+                    nsteps);
 }
 
 // --- ray bucketing by (instance, entry tile) ----------------------------------
@@ -921,7 +972,7 @@ WsLayout ws_layout(int nbins, long long np)
 template <typename KernelT>
 int occupancy_grid(KernelT kernel, int block, int slot)
 {
-    static int cache[6][64] = {{0}};
+    static int cache[9][64] = {{0}};
     int dev = 0;
     cudaGetDevice(&dev);
     int b = (dev >= 0 && dev < 64) ? cache[slot][dev] : 0;
@@ -947,7 +998,26 @@ int bin_grid(long long np)
     return (int)g;
 }
 
-// Bucket, then trace.  table.n == 1 runs the single-volume kernel.
+// True when every instance has instance 0's shape: the fields the uniform
+// batched kernel reads from entry 0 agree exactly.
+bool same_shape(const GeoTable& t)
+{
+    const Geo& a = t.g[0];
+    for (int i = 1; i < t.n; ++i) {
+        const Geo& b = t.g[i];
+        bool eq = a.tile_f4 == b.tile_f4 && a.sig_end == b.sig_end && a.extent == b.extent && a.st_b == b.st_b &&
+                  a.bd == b.bd && a.bd_shift == b.bd_shift && a.brick_f4 == b.brick_f4 && a.kappa == b.kappa &&
+                  a.sig_end_f == b.sig_end_f;
+        for (int k = 0; k < 3; ++k)
+            eq = eq && a.origin[k] == b.origin[k] && a.spacing[k] == b.spacing[k] &&
+                 a.inv_spacing[k] == b.inv_spacing[k] && a.n[k] == b.n[k] && a.axis[k] == b.axis[k] && a.r[k] == b.r[k];
+        if (!eq) return false;
+    }
+    return true;
+}
+
+// Bucket, then trace.  table.n == 1 runs the single-volume kernel, a batch of
+// one shape the uniform kernel, a batch of mixed shapes the mixed kernel.
 int run(const GeoTable& table, int nbins, const Ctl& K, int block, const double* s0, long long np, double* sf,
         double* rf, double* phase, int* status, int* nsteps, void* workspace, size_t workspace_bytes,
         cudaStream_t s, const char* who)
@@ -973,10 +1043,17 @@ int run(const GeoTable& table, int nbins, const Ctl& K, int block, const double*
 #define TT_LAUNCH_BATCH(BS, SLOT)                                                                     \
     trace32_batched_kernel<BS><<<occupancy_grid(trace32_batched_kernel<BS>, BS, SLOT), BS, 0, s>>>(  \
         table, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
+#define TT_LAUNCH_UNIFORM(BS, SLOT)                                                                   \
+    trace32_uniform_kernel<BS><<<occupancy_grid(trace32_uniform_kernel<BS>, BS, SLOT), BS, 0, s>>>(  \
+        table, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
     if (table.n == 1) {
         if (block == 64) TT_LAUNCH_SINGLE(64, 0);
         else if (block == 256) TT_LAUNCH_SINGLE(256, 2);
         else TT_LAUNCH_SINGLE(128, 1);
+    } else if (same_shape(table)) {
+        if (block == 64) TT_LAUNCH_UNIFORM(64, 6);
+        else if (block == 256) TT_LAUNCH_UNIFORM(256, 8);
+        else TT_LAUNCH_UNIFORM(128, 7);
     } else {
         if (block == 64) TT_LAUNCH_BATCH(64, 3);
         else if (block == 256) TT_LAUNCH_BATCH(256, 5);
@@ -984,6 +1061,7 @@ int run(const GeoTable& table, int nbins, const Ctl& K, int block, const double*
     }
 #undef TT_LAUNCH_SINGLE
 #undef TT_LAUNCH_BATCH
+#undef TT_LAUNCH_UNIFORM
     return tt::launch_status("trace_f32 kernel");
 }
 

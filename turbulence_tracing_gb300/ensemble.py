@@ -1,6 +1,12 @@
 """Batched ensemble: many field realisations of uneven grid size and ray count
-traced in ONE persistent launch, from a CUDA-graph-captured pipeline, with
-block size and brick depth chosen by the autotuner.
+traced by persistent batched launches from a CUDA-graph-captured pipeline,
+with block size and brick depth chosen by the autotuner.
+
+Instances are ordered by grid shape.  With grouped=True (default) each group
+of one shape is one persistent launch of the uniform-shape kernel (geometry
+in the constant bank, per-instance node buffer and ray block); with
+grouped=False all instances go through one launch of the mixed-shape kernel
+(per-lane geometry).
 
 Each instance gets a seeded band-limited Gaussian-random-field density
 (n^3 grid of side L, |k|^alpha, n_e = ne0 (1 + delta g)), a Gaussian beam
@@ -52,8 +58,11 @@ def gaussian_beam_into(dst, nrays, sigma, divergence, extent, rng):
 
 class Ensemble:
     def __init__(self, instances, L=2e-3, sigma_frac=0.25, divergence=0.05e-3, lwl=1064e-9, det=512,
-                 phase=False, rtol=1e-7, tune=True, tune_rays=200000, beam_seed=1):
-        self.inst = instances
+                 phase=False, rtol=1e-7, tune=True, tune_rays=200000, beam_seed=1, grouped=True):
+        order = sorted(range(len(instances)), key=lambda i: instances[i]["n"])
+        self.order = order  # instance k here is instances[order[k]]
+        self.inst = [instances[i] for i in order]
+        self.grouped = grouped
         self.L, self.sigma, self.div, self.lwl, self.det = L, sigma_frac * L, divergence, lwl, det
         self.phase, self.rtol = phase, rtol
         self.tune, self.tune_rays, self.beam_seed = tune, tune_rays, beam_seed
@@ -66,6 +75,13 @@ class Ensemble:
         self.offsets = np.zeros(n + 1, dtype=np.int64)
         for i, p in enumerate(self.inst):
             self.offsets[i + 1] = self.offsets[i] + p["nrays"]
+        # contiguous instance ranges of one grid shape
+        self.groups = []
+        for i, p in enumerate(self.inst):
+            if self.groups and self.inst[self.groups[-1][0]]["n"] == p["n"]:
+                self.groups[-1][1] = i + 1
+            else:
+                self.groups.append([i, i + 1])
         ntot = int(self.offsets[-1])
         self.ntot = ntot
         host = torch.empty(6 * ntot, dtype=torch.float64).pin_memory()
@@ -102,7 +118,7 @@ class Ensemble:
             self.vols.append(core.build_volume(self.fields[i], x, x, x, 2, lwl=self.lwl, brick_depth=bd))
         self.block = 128
         self.out = None
-        self.ws = None
+        self.ws = {}
         self.H = torch.zeros((n, self.det, self.det), dtype=torch.float64, device=dev)
         ext_mm = self.L * 1e3
         self.det_range = (-ext_mm, ext_mm)
@@ -122,9 +138,30 @@ class Ensemble:
             self.block = min(self.block_ms, key=self.block_ms.get)
         return self
 
+    def _launches(self):
+        """(instance range, ray range) of each batched launch."""
+        if not self.grouped:
+            return [((0, len(self.inst)), (0, int(self.offsets[-1])))]
+        return [((a, b), (int(self.offsets[a]), int(self.offsets[b]))) for a, b in self.groups]
+
     def _trace_only(self):
-        core.trace_f32_batched(self.vols, self.s0, self.offsets, self.t_ends, self.extents, rtol=self.rtol,
-                               phase=self.phase, out=self.out, ws=self.ws, block_size=self.block)
+        if self.out is None:
+            ntot = int(self.offsets[-1])
+            dev = self.s0.device
+            self.out = dict(sf=torch.empty(6 * ntot, dtype=torch.float64, device=dev),
+                            rf=torch.empty(4 * ntot, dtype=torch.float64, device=dev),
+                            phase=torch.empty(ntot, dtype=torch.float64, device=dev),
+                            status=torch.empty(ntot, dtype=torch.int32, device=dev),
+                            nsteps=torch.empty(ntot, dtype=torch.int32, device=dev))
+        for (a, b), (r0, r1) in self._launches():
+            if r1 == r0:
+                continue
+            view = {k: v[{"sf": 6, "rf": 4}.get(k, 1) * r0:{"sf": 6, "rf": 4}.get(k, 1) * r1]
+                    for k, v in self.out.items() if not k.startswith("_")}
+            o = core.trace_f32_batched(self.vols[a:b], self.s0[6 * r0:6 * r1], self.offsets[a:b + 1] - r0,
+                                       self.t_ends[a:b], self.extents[a:b], rtol=self.rtol, phase=self.phase,
+                                       out=view, ws=self.ws.get(a), block_size=self.block)
+            self.ws[a] = o["_ws"]
 
     # ------------------------------------------------------------------ one pass
     def step(self):
@@ -132,10 +169,7 @@ class Ensemble:
         after the first call, so it can be captured)."""
         for v in self.vols:
             core.rebuild_volume(v)
-        self.out = core.trace_f32_batched(self.vols, self.s0, self.offsets, self.t_ends, self.extents,
-                                          rtol=self.rtol, phase=self.phase, out=self.out, ws=self.ws,
-                                          block_size=self.block)
-        self.ws = self.out["_ws"]
+        self._trace_only()
         for i in range(len(self.inst)):
             rf = core.ray_block(self.out["rf"], 4, self.offsets, i)
             core.detect(rf, self.chain, self.det, self.det, self.det_range, self.det_range, H=self.H[i])

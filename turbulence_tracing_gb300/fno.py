@@ -127,6 +127,14 @@ class FNO:
                                           core._ptr(self.v), float(lr), float(beta1), float(beta2), float(eps),
                                           self.step_count, core._stream()), "tt_fno_adam")
 
+    def adam_device(self, lr_dev, step_dev, beta1=0.9, beta2=0.999, eps=1e-8):
+        """Adam with the learning rate and step counter in device tensors
+        (float32 (1,), int64 (1,)); the step is incremented on the device."""
+        _lib.check(_lib.lib().tt_fno_adam_device(self.n, core._ptr(self.params), core._ptr(self.grads),
+                                                 core._ptr(self.m), core._ptr(self.v), core._ptr(lr_dev),
+                                                 float(beta1), float(beta2), float(eps), core._ptr(step_dev),
+                                                 core._stream()), "tt_fno_adam_device")
+
     def error_flag(self):
         """1 if any bounded tensor-core wait ran out in any workspace (synchronises)."""
         flag = 0

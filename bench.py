@@ -70,6 +70,11 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-instances", type=int, default=64)
+    ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--sur-size", type=int, default=256)
+    ap.add_argument("--sur-train", type=int, default=2048)
+    ap.add_argument("--sur-test", type=int, default=96)
+    ap.add_argument("--sur-epochs", type=int, default=15)
     ap.add_argument("--json-out", default="")
     return ap.parse_args()
 
@@ -298,6 +303,9 @@ def run_ours(a):
         del out, wsp, vol
         torch.cuda.empty_cache()
         res["batched"] = batched_run(a)
+    if rank == 0 and not a.no_surrogate:
+        torch.cuda.empty_cache()
+        res["surrogate"] = surrogate_run(a)
     if rank == 0 and not a.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(a, ne, x)
     if dist:
@@ -374,48 +382,139 @@ def batched_run(a):
     """The batched ensemble: a.batch_instances realisations drawn as the batched
     workload (grid 128/192/256/384^3, exponent -5/3/-3/-11/3, delta in
     [0.05, 0.3], background 1e23..1e25 m^-3, 1e5..4e6 rays log-uniform,
-    sigma 0.25 L, 0.05 mrad, L = 2 mm, 512^2 shadowgram each), traced in one
-    persistent launch replayed from a CUDA graph, against the same work as one
-    launch per instance without a graph."""
+    sigma 0.25 L, 0.05 mrad, L = 2 mm, 512^2 shadowgram each).  Pipeline per
+    step, one CUDA graph: volume builds, ray bucketing, the persistent trace
+    launches, shadowgrams.  The ensemble's set-up times the launch modes on
+    the ensemble itself (one batched launch per grid shape, or one launch per
+    instance) and keeps the faster; the single mixed-shape launch and the
+    eager one-launch-per-instance form are timed beside it.  The same is
+    repeated for small instances (2e3..8e4 rays)."""
     import torch
 
     from turbulence_tracing_gb300 import ensemble
 
-    inst = ensemble.draw_instances(a.batch_instances, seed=a.seed)
-    E = ensemble.Ensemble(inst, L=2e-3, det=512, phase=False, tune=True).setup()
-    E.capture()
-    for _ in range(2):
-        E.replay()
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def one(inst):
+        E = ensemble.Ensemble(inst, L=2e-3, det=512, phase=False, tune=True).setup()
+        E.capture()
+        ms = timed(E.replay)
+        steps = E.ray_steps()
+        bad = int((E.out["status"] != 0).sum().item())
+        chosen = E.mode
+        trace_ms = {m: E.mode_ms[m] for m in E.mode_ms}
+        E.mode = "one_launch"
+        trace_ms["one_launch"] = timed(E._trace_only, 2)
+        E.mode = chosen
+        ms_eager = timed(E.run_unbatched, 1)
+        r = {"instances": len(inst), "rays": E.ntot, "ray_steps_per_step": steps, "mode": chosen,
+             "launches": len(E._launches()), "block_size": E.block, "graph_ms_per_step": ms,
+             "ray_steps_per_s": steps / (ms / 1e3), "rays_per_s": E.ntot / (ms / 1e3), "non_ok_rays": bad,
+             "trace_only_ms_by_mode": trace_ms, "eager_one_launch_per_instance_ms_per_step": ms_eager,
+             "speedup_vs_eager_per_instance": ms_eager / ms}
+        sizes = {}
+        for p in inst:
+            sizes[p["n"]] = sizes.get(p["n"], 0) + 1
+        r["grid_counts"] = {str(k): v for k, v in sorted(sizes.items())}
+        r["autotuned_per_grid"] = {str(k): {"block": v["block"], "brick_depth": v["brick_depth"]}
+                                   for k, v in E.tuned.items()}
+        del E
+        torch.cuda.empty_cache()
+        return r
+
+    out = one(ensemble.draw_instances(a.batch_instances, seed=a.seed))
+    out["small_instances"] = one(ensemble.draw_instances(a.batch_instances, seed=a.seed, rays=(2e3, 8e4)))
+    out["pipeline"] = "CUDA graph: volume builds + bucketing + persistent trace launches + shadowgrams"
+    return out
+
+
+def surrogate_run(a):
+    """The learned surrogate (straight-line maps -> full-trace deflection and
+    phase correction) at a.sur_size^2 on fields drawn as the batched workload
+    at that grid: data made by the tracer itself, FNO training by the
+    library's kernels, held-out evaluation against the exact tracer, then the
+    surrogate-with-fallback pipeline timed against tracing every field."""
+    import time
+
+    import torch
+
+    from turbulence_tracing_gb300 import fno, surrogate as SG
+
+    S = a.sur_size
+    W = SG.Workload(S)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    X, Y, _, _, steps_tr = SG.build_dataset(W, SG.draw_fields(a.sur_train, seed=a.seed + 11))
+    Xte, _, ste, truth, _ = SG.build_dataset(W, SG.draw_fields(a.sur_test, seed=a.seed + 12), keep_truth=True)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    net = fno.FNO(S, in_ch=SG.IN_CH, out_ch=3, layers=4, seed=a.seed)
+    trainer = SG.Trainer(net, X, Y, batch=8)
+    hist, sps = trainer.fit(a.sur_epochs, lr=1e-3)
+    res = SG.evaluate(W, net, Xte, ste, truth)
+    half = len(res) // 2
+    kappa = SG.calibrate(res[:half])
+    held = res[half:]
+
+    def mean(k):
+        return float(np.mean([r[k] for r in held]))
+
+    # inference kernel throughput: forward passes of a batch of 8
+    xb = Xte[:8].contiguous()
+    ob = net.forward(xb)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    reps = 3
     e0.record()
-    for _ in range(reps):
-        E.replay()
+    for _ in range(10):
+        net.forward(xb, out=ob)
     e1.record()
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    steps = E.ray_steps()
-    bad = int((E.out["status"] != 0).sum().item())
-    E.run_unbatched()
+    us_fwd = e0.elapsed_time(e1) * 1e3 / 80
+    C = 32
+    fwd_bytes = 4 * (6 * C * S * S * 1 + 16 * C * 32 * S) + (4 * SG.IN_CH + 2 * C) * S * S + (2 * C + 12) * S * S
+    peak, peak_kind = peaks()
+    # the pipeline against tracing every held-out field
+    params = SG.draw_fields(a.sur_test, seed=a.seed + 12)[half:]
+    fields = [W.field(p) for p in params]
+    pipe = SG.Pipeline(W, net, kappa)
+    pipe.run(fields[:2])
+    pipe.run_tracer(fields[:2])
     torch.cuda.synchronize()
-    e0.record()
-    E.run_unbatched()
-    e1.record()
+    t0 = time.perf_counter()
+    I_p, fell = pipe.run(fields)
     torch.cuda.synchronize()
-    ms_unb = e0.elapsed_time(e1)
-    sizes = {}
-    for p in inst:
-        sizes[p["n"]] = sizes.get(p["n"], 0) + 1
-    return {"instances": len(inst), "rays": E.ntot, "grid_counts": {str(k): v for k, v in sorted(sizes.items())},
-            "ray_steps_per_step": steps, "ms_per_step": ms, "ray_steps_per_s": steps / (ms / 1e3),
-            "rays_per_s": E.ntot / (ms / 1e3), "non_ok_rays": bad,
-            "unbatched_ms_per_step": ms_unb, "speedup_vs_one_launch_per_instance": ms_unb / ms,
-            "block_size": E.block, "block_ms": {str(k): v for k, v in getattr(E, "block_ms", {}).items()},
-            "autotuned_per_grid": {str(k): {"block": v["block"], "brick_depth": v["brick_depth"]}
-                                   for k, v in E.tuned.items()},
-            "pipeline": "CUDA graph: 64 volume builds + bucketing + one batched trace launch + 64 shadowgrams"}
+    t_pipe = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    I_t = pipe.run_tracer(fields)
+    torch.cuda.synchronize()
+    t_tr = time.perf_counter() - t0
+    errs = [SG.rel_l2(p_, t_) for p_, t_ in zip(I_p, I_t)]
+    acc = [e for e, f in zip(errs, fell) if not f]
+    return {"grid": S, "train_fields": a.sur_train, "test_fields": a.sur_test, "epochs": a.sur_epochs,
+            "data_s": t_data, "train_samples_per_s": sps, "loss_first_last": [hist[0], hist[-1]],
+            "heldout": {"shadow_err_straight": mean("err_straight"), "shadow_err_net": mean("err_net"),
+                        "theta_err_straight": mean("theta_err_straight"), "theta_err_net": mean("theta_err_net"),
+                        "phase_corr_err_net": mean("phase_corr_err_net"), "fields": len(held)},
+            "fno_forward_us_per_field": us_fwd,
+            "fno_forward_roofline": {"bound": "hbm", "achieved": fwd_bytes / (us_fwd * 1e-6) / 1e9, "peak": peak,
+                                     "unit": "GB/s", "frac": fwd_bytes / (us_fwd * 1e-6) / 1e9 / peak,
+                                     "bytes_per_field": fwd_bytes, "peak_kind": peak_kind},
+            "pipeline": {"kappa": kappa, "tol": 0.02, "fallback_fraction": float(np.mean(fell)),
+                         "accepted_err_max": max(acc) if acc else None,
+                         "accepted_err_mean": float(np.mean(acc)) if acc else None,
+                         "pipeline_s": t_pipe, "tracer_only_s": t_tr, "speedup_vs_tracer": t_tr / t_pipe},
+            "error_flag": net.error_flag()}
 
 
 def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):

@@ -21,12 +21,12 @@ def _small_ensemble(**kw):
     return ensemble.Ensemble(inst, L=1e-3, det=64, phase=True, **kw).setup()
 
 
-@pytest.mark.parametrize("grouped", [True, False])
-def test_batched_equals_single_launches(cuda, grouped):
-    """grouped: one uniform-shape launch per grid size; else one mixed-shape launch."""
+@pytest.mark.parametrize("mode", ["grouped", "one_launch"])
+def test_batched_equals_single_launches(cuda, mode):
+    """grouped: one uniform-shape launch per grid size; one_launch: one mixed-shape launch."""
     from turbulence_tracing_gb300 import core
 
-    E = _small_ensemble(tune=False, grouped=grouped)
+    E = _small_ensemble(tune=False, mode=mode)
     torch.cuda.synchronize()
     rf_b = E.out["rf"].clone()
     ph_b = E.out["phase"].clone()

@@ -53,7 +53,8 @@ class TTVolume(ctypes.Structure):
 
 class TTTraceOpts(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double), ("atol_phase", ctypes.c_double),
-                ("max_steps", ctypes.c_int64), ("with_phase", ctypes.c_int32), ("block_size", ctypes.c_int32)]
+                ("max_steps", ctypes.c_int64), ("with_phase", ctypes.c_int32), ("block_size", ctypes.c_int32),
+                ("ray_chunk", ctypes.c_int32)]
 
 
 class TTFnoDims(ctypes.Structure):

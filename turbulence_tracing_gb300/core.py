@@ -159,7 +159,7 @@ def rebuild_volume(vol):
 # ---------------------------------------------------------------------------
 # K2
 # ---------------------------------------------------------------------------
-def _opts(rtol, atol, atol_phase, max_steps, with_phase, block_size=0):
+def _opts(rtol, atol, atol_phase, max_steps, with_phase, block_size=0, ray_chunk=0):
     o = _lib.TTTraceOpts()
     o.rtol = float(rtol)
     o.atol = float(atol)
@@ -167,6 +167,7 @@ def _opts(rtol, atol, atol_phase, max_steps, with_phase, block_size=0):
     o.max_steps = int(max_steps or 0)
     o.with_phase = 1 if with_phase else 0
     o.block_size = int(block_size or 0)
+    o.ray_chunk = int(ray_chunk or 0)
     return o
 
 
@@ -199,7 +200,7 @@ def trace_f64(fields, s0, t_end, probing_axis, extent, rtol=1e-3, atol=1e-6, pha
 
 
 def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, phase=False, max_steps=None,
-              want_sf=True, ws=None, out=None, block_size=0):
+              want_sf=True, ws=None, out=None, block_size=0, ray_chunk=0):
     """Persistent FP32 tracer over a Volume32.  s0: (6, Np) float64."""
     dev = require_cuda()
     L = _lib.lib()
@@ -212,7 +213,7 @@ def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, pha
     need = L.tt_trace_f32_workspace_bytes(ctypes.byref(vol.desc), np_)
     if ws is None or ws.numel() < need:
         ws = workspace(need, dev)
-    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size)
+    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size, ray_chunk)
     check(L.tt_trace_f32(ctypes.byref(vol.desc), _ptr(s0_t), np_, float(t_end), float(extent), ctypes.byref(o),
                          _ptr(out["sf"]), _ptr(out["rf"]), _ptr(out["phase"]) if phase else None,
                          _ptr(out["status"]), _ptr(out["nsteps"]), _ptr(ws), ws.numel(), _stream()),
@@ -222,7 +223,7 @@ def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, pha
 
 
 def trace_f32_batched(vols, s0, ray_offsets, t_ends, extents, rtol=1e-7, atol=1e-5, atol_phase=1e-5,
-                      phase=False, max_steps=None, want_sf=True, ws=None, out=None, block_size=0):
+                      phase=False, max_steps=None, want_sf=True, ws=None, out=None, block_size=0, ray_chunk=0):
     """All instances in one persistent launch.  s0 is the instance-blocked ray
     array: a flat float64 tensor holding instance i's (6, n_i) block at
     6 * ray_offsets[i].  Outputs are blocked the same way (see ray_block)."""
@@ -249,7 +250,7 @@ def trace_f32_batched(vols, s0, ray_offsets, t_ends, extents, rtol=1e-7, atol=1e
     need = L.tt_trace_f32_batched_workspace_bytes(descs, n, ntot)
     if ws is None or ws.numel() < need:
         ws = workspace(need, dev)
-    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size)
+    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size, ray_chunk)
     dp = ctypes.POINTER(ctypes.c_double)
     check(L.tt_trace_f32_batched(descs, n, offs.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), te.ctypes.data_as(dp),
                                  ex.ctypes.data_as(dp), _ptr(s0_t), ctypes.byref(o), _ptr(out["sf"]), _ptr(out["rf"]),

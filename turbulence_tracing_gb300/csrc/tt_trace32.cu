@@ -110,6 +110,7 @@ struct Geo {
 struct Ctl {
     float rtol, inv_rtol, inv_atol_cells, atol_phase;
     int with_phase;
+    int chunk;  // rays a warp takes from the work counter at a time (>= 32)
     long long max_steps;
 };
 
@@ -699,46 +700,76 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
                                                 double* __restrict__ rf, double* __restrict__ phase,
                                                 int* __restrict__ status, int* __restrict__ nsteps)
 {
+    // perm positions and ray indices fit in 32 bits (the host keeps np <= 2^32 - 2^16)
     const unsigned lane = threadIdx.x & 31u;
-    long long idx = -1;      // position in perm of this lane's ray
-    long long ray = 0;
+    const unsigned n32 = (unsigned)np;
+    bool busy = false;        // this lane holds a ray
+    unsigned ray = 0;
     bool drained = false;
+    unsigned wnext = 0, wend = 0;  // the warp's chunk of perm positions (warp-uniform)
     const float4* nodes = nullptr;
     Ray R;
     double P0[3], u0[3];
     float coef[4][8];
     R.state = 1;
     for (;;) {
-        const bool need = (idx < 0) && !drained;
+        const bool need = !busy && !drained;
         const unsigned mask = __ballot_sync(0xffffffffu, need);
         if (mask) {
-            unsigned long long base = 0;
-            const int leader = __ffs(mask) - 1;
-            if ((int)lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
-            base = __shfl_sync(0xffffffffu, base, leader);
+            // lanes are refilled from the warp's chunk of consecutive bucketed
+            // rays; a new chunk comes from the shared work counter.  (Larger
+            // chunks, and per-block segments with stealing, both measured slower.)
+            const unsigned cnt = __popc(mask);
+            const unsigned avail = wend - wnext;
+            unsigned nb = 0, ne = 0;
+            if (avail < cnt) {
+                const int leader = __ffs(mask) - 1;
+                if ((int)lane == leader) {
+                    nb = ne = n32;
+                    const unsigned long long got = atomicAdd(counter, (unsigned long long)K.chunk);
+                    if (got < n32) {
+                        nb = (unsigned)got;
+                        ne = (unsigned)(got + K.chunk < n32 ? got + K.chunk : n32);
+                    }
+                }
+                nb = __shfl_sync(0xffffffffu, nb, leader);
+                ne = __shfl_sync(0xffffffffu, ne, leader);
+            }
             if (need) {
-                const unsigned long long my = base + __popc(mask & ((1u << lane) - 1u));
-                if (my < (unsigned long long)np) {
-                    idx = (long long)my;
-                    ray = perm ? (long long)perm[idx] : idx;
+                const unsigned rank = __popc(mask & ((1u << lane) - 1u));
+                bool got = rank < avail;
+                unsigned my = wnext + rank;
+                if (!got) {
+                    my = nb + (rank - avail);
+                    got = my < ne;
+                }
+                if (got) {
+                    ray = perm ? perm[my] : my;
+                    busy = true;
                     const Src src = pol.src(ray);
                     nodes = src.nodes;
                     if (!init_ray(pol.geo(ray), src, s0, np, ray, R, P0, u0)) {
                         finish_ray(pol.geo(ray), src, R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
-                        idx = -1;  // picked up again on the next pass
+                        busy = false;  // picked up again on the next pass
                     }
-                } else {
-                    drained = true;
+                } else if (nb == ne) {
+                    drained = true;  // no ray left anywhere
                 }
             }
+            if (avail < cnt) {
+                const unsigned take = cnt - avail < ne - nb ? cnt - avail : ne - nb;
+                wnext = nb + take;
+                wend = ne;
+            } else {
+                wnext += cnt;
+            }
         }
-        const bool active = idx >= 0;
-        if (__ballot_sync(0xffffffffu, active || (!drained)) == 0u) break;
-        if (active) {
+        if (__ballot_sync(0xffffffffu, busy || (!drained)) == 0u) break;
+        if (busy) {
             step(pol.geo(ray), pol.nodes(nodes), K, T, R, coef);
             if (R.state != 0) {
                 finish_ray(pol.geo(ray), pol.src(ray), R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
-                idx = -1;
+                busy = false;
             }
         }
     }
@@ -948,6 +979,9 @@ int make_ctl(const tt_trace_opts* opts, Ctl* K)
     K->atol_phase = (float)(opts->with_phase ? opts->atol_phase : 1.0);
     K->with_phase = opts->with_phase ? 1 : 0;
     K->max_steps = opts->max_steps > 0 ? opts->max_steps : TT_DEFAULT_MAX_STEPS;
+    const int ch = opts->ray_chunk;
+    if (ch != 0 && (ch < 32 || ch > 1024 || ch % 32)) return tt::invalid("trace_f32: ray_chunk must be 0 or 32..1024, a multiple of 32");
+    K->chunk = ch ? ch : 32;  // 32 measured fastest
     return TT_OK;
 }
 
@@ -1037,15 +1071,16 @@ int run(const GeoTable& table, int nbins, const Ctl& K, int block, const double*
     bin_scatter_kernel<<<bin_grid(np), 256, 0, s>>>(table, s0, np, cnt, perm);
     TT_TRY(tt::launch_status("trace_f32 ray binning"));
     const Tab& T = tableau();
+    const Ctl& Kc = K;
 #define TT_LAUNCH_SINGLE(BS, SLOT)                                                                    \
     trace32_kernel<BS><<<occupancy_grid(trace32_kernel<BS>, BS, SLOT), BS, 0, s>>>(                  \
-        table.g[0], K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
+        table.g[0], Kc, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
 #define TT_LAUNCH_BATCH(BS, SLOT)                                                                     \
     trace32_batched_kernel<BS><<<occupancy_grid(trace32_batched_kernel<BS>, BS, SLOT), BS, 0, s>>>(  \
-        table, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
+        table, Kc, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
 #define TT_LAUNCH_UNIFORM(BS, SLOT)                                                                   \
     trace32_uniform_kernel<BS><<<occupancy_grid(trace32_uniform_kernel<BS>, BS, SLOT), BS, 0, s>>>(  \
-        table, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
+        table, Kc, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
     if (table.n == 1) {
         if (block == 64) TT_LAUNCH_SINGLE(64, 0);
         else if (block == 256) TT_LAUNCH_SINGLE(256, 2);
@@ -1085,7 +1120,7 @@ extern "C" int tt_trace_f32(const tt_volume* vol, const double* s0, int64_t np, 
 {
     if (!vol || !opts) return tt::invalid("trace_f32: null volume or opts");
     if (np < 0) return tt::invalid("trace_f32: np < 0");
-    if (np > 0xffffffffLL) return tt::invalid("trace_f32: at most 2^32-1 rays per call");
+    if (np > 0xffff0000LL) return tt::invalid("trace_f32: at most 2^32 - 2^16 rays per call");
     GeoTable& H = host_table();
     H.n = 1;
     TT_TRY(make_geo(vol, t_end, extent, 0, np, 0, &H.g[0]));
@@ -1117,7 +1152,7 @@ extern "C" int tt_trace_f32_batched(const tt_volume* vols, int ninst, const int6
     for (int i = 0; i < ninst; ++i)
         if (ray_offsets[i + 1] < ray_offsets[i]) return tt::invalid("trace_f32_batched: ray_offsets must not decrease");
     const long long np = ray_offsets[ninst];
-    if (np > 0xffffffffLL) return tt::invalid("trace_f32_batched: at most 2^32-1 rays per call");
+    if (np > 0xffff0000LL) return tt::invalid("trace_f32_batched: at most 2^32 - 2^16 rays per call");
     Ctl K;
     TT_TRY(make_ctl(opts, &K));
     GeoTable& H = host_table();

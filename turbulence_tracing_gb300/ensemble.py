@@ -2,11 +2,18 @@
 traced by persistent batched launches from a CUDA-graph-captured pipeline,
 with block size and brick depth chosen by the autotuner.
 
-Instances are ordered by grid shape.  With grouped=True (default) each group
-of one shape is one persistent launch of the uniform-shape kernel (geometry
-in the constant bank, per-instance node buffer and ray block); with
-grouped=False all instances go through one launch of the mixed-shape kernel
-(per-lane geometry).
+Instances are ordered by grid shape.  Launch modes:
+  grouped       one persistent launch per grid shape (uniform-shape kernel:
+                geometry in the constant bank, per-instance node buffer and
+                ray block)
+  one_launch    every instance in one launch of the mixed-shape kernel
+                (per-lane geometry)
+  per_instance  one launch per instance
+With tune=True the set-up times grouped and per_instance on the ensemble
+itself and keeps the faster: batching wins when instances are small (launch
+tails and launch overhead dominate), separate launches when they are large
+(each launch starts with all lanes on neighbouring rays, which keeps the
+cache hit rate up).
 
 Each instance gets a seeded band-limited Gaussian-random-field density
 (n^3 grid of side L, |k|^alpha, n_e = ne0 (1 + delta g)), a Gaussian beam
@@ -58,11 +65,13 @@ def gaussian_beam_into(dst, nrays, sigma, divergence, extent, rng):
 
 class Ensemble:
     def __init__(self, instances, L=2e-3, sigma_frac=0.25, divergence=0.05e-3, lwl=1064e-9, det=512,
-                 phase=False, rtol=1e-7, tune=True, tune_rays=200000, beam_seed=1, grouped=True):
+                 phase=False, rtol=1e-7, tune=True, tune_rays=200000, beam_seed=1, mode="grouped"):
         order = sorted(range(len(instances)), key=lambda i: instances[i]["n"])
         self.order = order  # instance k here is instances[order[k]]
         self.inst = [instances[i] for i in order]
-        self.grouped = grouped
+        if mode not in ("grouped", "one_launch", "per_instance"):
+            raise ValueError("mode must be grouped, one_launch or per_instance")
+        self.mode = mode
         self.L, self.sigma, self.div, self.lwl, self.det = L, sigma_frac * L, divergence, lwl, det
         self.phase, self.rtol = phase, rtol
         self.tune, self.tune_rays, self.beam_seed = tune, tune_rays, beam_seed
@@ -130,7 +139,12 @@ class Ensemble:
         self.step()  # allocates outputs and workspace once
         torch.cuda.synchronize()
         if self.tune:
-            # the batched launch has one block size for all instances: time the batch itself
+            # launch mode, then the block size of the chosen mode, timed on the ensemble itself
+            self.mode_ms = {}
+            for m in ("grouped", "per_instance"):
+                self.mode = m
+                self.mode_ms[m] = autotune._time(self._trace_only, 1)
+            self.mode = min(self.mode_ms, key=self.mode_ms.get)
             self.block_ms = {}
             for b in autotune.BLOCKS:
                 self.block = b
@@ -140,9 +154,13 @@ class Ensemble:
 
     def _launches(self):
         """(instance range, ray range) of each batched launch."""
-        if not self.grouped:
-            return [((0, len(self.inst)), (0, int(self.offsets[-1])))]
-        return [((a, b), (int(self.offsets[a]), int(self.offsets[b]))) for a, b in self.groups]
+        if self.mode == "one_launch":
+            ranges = [(0, len(self.inst))]
+        elif self.mode == "per_instance":
+            ranges = [(i, i + 1) for i in range(len(self.inst))]
+        else:
+            ranges = [tuple(g) for g in self.groups]
+        return [((a, b), (int(self.offsets[a]), int(self.offsets[b]))) for a, b in ranges]
 
     def _trace_only(self):
         if self.out is None:
@@ -160,8 +178,8 @@ class Ensemble:
                     for k, v in self.out.items() if not k.startswith("_")}
             o = core.trace_f32_batched(self.vols[a:b], self.s0[6 * r0:6 * r1], self.offsets[a:b + 1] - r0,
                                        self.t_ends[a:b], self.extents[a:b], rtol=self.rtol, phase=self.phase,
-                                       out=view, ws=self.ws.get(a), block_size=self.block)
-            self.ws[a] = o["_ws"]
+                                       out=view, ws=self.ws.get((self.mode, a)), block_size=self.block)
+            self.ws[(self.mode, a)] = o["_ws"]
 
     # ------------------------------------------------------------------ one pass
     def step(self):
@@ -207,3 +225,34 @@ class Ensemble:
 
     def ray_steps(self):
         return int(self.out["nsteps"].sum().item())
+
+
+def _main(argv=None):
+    """Trace an ensemble once in each launch mode and print the timings:
+    python -m turbulence_tracing_gb300.ensemble --instances 8 --grid 128 --rays 2e5"""
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description=_main.__doc__)
+    ap.add_argument("--instances", type=int, default=8)
+    ap.add_argument("--grid", type=int, default=0, help="one grid size for all instances (0: drawn)")
+    ap.add_argument("--rays", type=float, default=0, help="rays per instance (0: drawn)")
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--reps", type=int, default=2)
+    a = ap.parse_args(argv)
+    inst = draw_instances(a.instances, seed=a.seed)
+    for p in inst:
+        if a.grid:
+            p["n"] = a.grid
+        if a.rays:
+            p["nrays"] = int(a.rays)
+    E = Ensemble(inst, tune=False).setup()
+    res = {}
+    for m in ("grouped", "one_launch", "per_instance"):
+        E.mode = m
+        res[m] = autotune._time(E._trace_only, a.reps)
+    print(json.dumps({"instances": len(inst), "rays": E.ntot, "trace_ms_by_mode": res}))
+
+
+if __name__ == "__main__":
+    _main()

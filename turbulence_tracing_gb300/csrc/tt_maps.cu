@@ -18,32 +18,18 @@
 
 namespace {
 
+// One warp per pixel: lane l handles nodes k = l, l + 32, ... along z, so
+// the column reads (z is the fastest axis of the density) are coalesced; the
+// per-lane sums are combined with shuffles.
 template <typename T>
-__device__ __forceinline__ float qval(const T* __restrict__ ne, int i, int j, int k, int ny, int nz, float inv_nc,
-                                      float ne_max)
-{
-    const float q = (float)ne[((size_t)i * ny + j) * nz + k] * inv_nc;
-    return q < ne_max ? q : ne_max;
-}
-
-// numpy.gradient along one axis at index i of n, unit spacing (the caller divides by h).
-template <typename F>
-__device__ __forceinline__ float grad1(F f, int i, int n)
-{
-    if (i == 0) return f(1) - f(0);
-    if (i == n - 1) return f(n - 1) - f(n - 2);
-    return 0.5f * (f(i + 1) - f(i - 1));
-}
-
-template <typename T>
-__global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, double x0, double hx, double y0,
-                            double hy, double hz, float inv_nc, float ne_max, double k0, int P, int nout,
-                            float* __restrict__ out)
+__global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, double hx, double hy, double hz,
+                            float inv_nc, float ne_max, double k0, int P, int nout, float* __restrict__ out)
 {
     const int n = P * P;
-    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= n) return;
-    const int pi = pix / P, pj = pix % P;
+    const int warp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const int pi = warp / P, pj = warp % P;
     const double xs = ((pi + 0.5) / P) * (hx * (nx - 1));
     const double ys = ((pj + 0.5) / P) * (hy * (ny - 1));
     int ix = (int)floor(xs / hx), iy = (int)floor(ys / hy);
@@ -51,48 +37,66 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
     iy = iy < 0 ? 0 : (iy > ny - 2 ? ny - 2 : iy);
     const float fx = (float)(xs / hx - ix), fy = (float)(ys / hy - iy);
     const float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w01 = (1.f - fx) * fy, w11 = fx * fy;
-    double sx = 0.0, sy = 0.0, sp = 0.0, mx = 0.0, my = 0.0;
-    float qprev = 0.f;
     const float gw[4] = {0.0694318442029737f, 0.3300094782075719f, 0.6699905217924281f, 0.9305681557970263f};
     const float gwt[4] = {0.1739274225687269f, 0.3260725774312731f, 0.3260725774312731f, 0.1739274225687269f};
-    for (int k = 0; k < nz; ++k) {
-        auto q = [&](int i, int j) { return qval(ne, i, j, k, ny, nz, inv_nc, ne_max); };
-        const float gx0 = grad1([&](int i) { return q(i, iy); }, ix, nx);
-        const float gx1 = grad1([&](int i) { return q(i, iy); }, ix + 1, nx);
-        const float gx2 = grad1([&](int i) { return q(i, iy + 1); }, ix, nx);
-        const float gx3 = grad1([&](int i) { return q(i, iy + 1); }, ix + 1, nx);
-        const float gy0 = grad1([&](int j) { return q(ix, j); }, iy, ny);
-        const float gy1 = grad1([&](int j) { return q(ix + 1, j); }, iy, ny);
-        const float gy2 = grad1([&](int j) { return q(ix, j); }, iy + 1, ny);
-        const float gy3 = grad1([&](int j) { return q(ix + 1, j); }, iy + 1, ny);
+    // columns: x neighbours ix-1..ix+2 at rows iy, iy+1; y neighbours iy-1..iy+2 at columns ix, ix+1
+    const int xm = ix > 0 ? ix - 1 : ix, xp = ix + 2 < nx ? ix + 2 : ix + 1;
+    const int ym = iy > 0 ? iy - 1 : iy, yp = iy + 2 < ny ? iy + 2 : iy + 1;
+    auto col = [&](int i, int j) { return ne + ((size_t)i * ny + j) * nz; };
+    const T *c00 = col(ix, iy), *c10 = col(ix + 1, iy), *c01 = col(ix, iy + 1), *c11 = col(ix + 1, iy + 1);
+    const T *cxm0 = col(xm, iy), *cxp0 = col(xp, iy), *cxm1 = col(xm, iy + 1), *cxp1 = col(xp, iy + 1);
+    const T *cym0 = col(ix, ym), *cyp0 = col(ix, yp), *cym1 = col(ix + 1, ym), *cyp1 = col(ix + 1, yp);
+    // numpy.gradient (unit spacing): central inside, one-sided at the faces
+    const float dx0 = ix > 0 ? 0.5f : 1.f, dx1 = ix + 2 < nx ? 0.5f : 1.f;
+    const float dy0 = iy > 0 ? 0.5f : 1.f, dy1 = iy + 2 < ny ? 0.5f : 1.f;
+    auto q = [&](const T* c, int k) {
+        const float v = (float)c[k] * inv_nc;
+        return v < ne_max ? v : ne_max;
+    };
+    float sx = 0.f, sy = 0.f, mx = 0.f, my = 0.f, sp = 0.f;
+    for (int k = lane; k < nz; k += 32) {
+        const float q00 = q(c00, k), q10 = q(c10, k), q01 = q(c01, k), q11 = q(c11, k);
+        // d/dx at (ix, .) uses (ix+1) - (ix-1) (or the one-sided pair), at (ix+1, .) uses (ix+2) - ix
+        const float gx0 = dx0 * (q10 - q(cxm0, k)), gx1 = dx1 * (q(cxp0, k) - q00);
+        const float gx2 = dx0 * (q11 - q(cxm1, k)), gx3 = dx1 * (q(cxp1, k) - q01);
+        const float gy0 = dy0 * (q01 - q(cym0, k)), gy2 = dy1 * (q(cyp0, k) - q00);
+        const float gy1 = dy0 * (q11 - q(cym1, k)), gy3 = dy1 * (q(cyp1, k) - q10);
         const float gxk = w00 * gx0 + w10 * gx1 + w01 * gx2 + w11 * gx3;
         const float gyk = w00 * gy0 + w10 * gy1 + w01 * gy2 + w11 * gy3;
-        const float qk = w00 * q(ix, iy) + w10 * q(ix + 1, iy) + w01 * q(ix, iy + 1) + w11 * q(ix + 1, iy + 1);
-        const double wz = (k == 0 || k == nz - 1) ? 0.5 : 1.0;
-        sx += wz * gxk;
-        sy += wz * gyk;
-        // first moment, trapezoid rule on the nodes
-        const double zr = (double)k / (double)(nz - 1);
-        mx += wz * zr * gxk;
-        my += wz * zr * gyk;
-        if (k > 0) {
+        const float wz = (k == 0 || k == nz - 1) ? 0.5f : 1.f;
+        const float zr = (float)k / (float)(nz - 1);
+        sx = fmaf(wz, gxk, sx);
+        sy = fmaf(wz, gyk, sy);
+        mx = fmaf(wz * zr, gxk, mx);
+        my = fmaf(wz * zr, gyk, my);
+        if (k + 1 < nz) {  // the cell [k, k+1]: 4-point Gauss-Legendre on the linear q(z)
+            const float qk = w00 * q00 + w10 * q10 + w01 * q01 + w11 * q11;
+            const float qn = w00 * q(c00, k + 1) + w10 * q(c10, k + 1) + w01 * q(c01, k + 1) + w11 * q(c11, k + 1);
             float cell = 0.f;
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
-                const float qq = qprev + gw[g] * (qk - qprev);
-                const float r = 1.f - qq;
+                const float r = 1.f - (qk + gw[g] * (qn - qk));
                 cell += gwt[g] * (sqrtf(r > 0.f ? r : 0.f) - 1.f);
             }
             sp += cell;
         }
-        qprev = qk;
     }
-    out[pix] = (float)(-0.5 * sx * hz / hx);
-    out[n + pix] = (float)(-0.5 * sy * hz / hy);
-    out[2 * n + pix] = (float)(k0 * sp * hz);
-    if (nout > 3) {
-        out[3 * n + pix] = (float)(-0.5 * mx * hz / hx);
-        out[4 * n + pix] = (float)(-0.5 * my * hz / hy);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, off);
+        sy += __shfl_xor_sync(0xffffffffu, sy, off);
+        mx += __shfl_xor_sync(0xffffffffu, mx, off);
+        my += __shfl_xor_sync(0xffffffffu, my, off);
+        sp += __shfl_xor_sync(0xffffffffu, sp, off);
+    }
+    if (lane == 0) {
+        out[warp] = (float)(-0.5 * (double)sx * hz / hx);
+        out[n + warp] = (float)(-0.5 * (double)sy * hz / hy);
+        out[2 * n + warp] = (float)(k0 * (double)sp * hz);
+        if (nout > 3) {
+            out[3 * n + warp] = (float)(-0.5 * (double)mx * hz / hx);
+            out[4 * n + warp] = (float)(-0.5 * (double)my * hz / hy);
+        }
     }
 }
 
@@ -113,14 +117,15 @@ extern "C" int tt_straight_line_maps(const void* ne, int ne_dtype, int nx, int n
     const double nc = 3.14207787e-4 * omega * omega;
     const double k0 = omega / TT_C_LIGHT;
     const int n = P * P;
-    const int grid = (n + 127) / 128;
+    const long long threads = (long long)n * 32;
+    const int grid = (int)((threads + 255) / 256);
     cudaStream_t s = tt::as_stream(stream);
     if (ne_dtype == TT_F32)
-        maps_kernel<float><<<grid, 128, 0, s>>>((const float*)ne, nx, ny, nz, x[0], hx, y[0], hy, hz,
-                                                (float)(1.0 / nc), (float)ne_max, k0, P, nout, out);
+        maps_kernel<float><<<grid, 256, 0, s>>>((const float*)ne, nx, ny, nz, hx, hy, hz, (float)(1.0 / nc),
+                                                (float)ne_max, k0, P, nout, out);
     else
-        maps_kernel<double><<<grid, 128, 0, s>>>((const double*)ne, nx, ny, nz, x[0], hx, y[0], hy, hz,
-                                                 (float)(1.0 / nc), (float)ne_max, k0, P, nout, out);
+        maps_kernel<double><<<grid, 256, 0, s>>>((const double*)ne, nx, ny, nz, hx, hy, hz, (float)(1.0 / nc),
+                                                 (float)ne_max, k0, P, nout, out);
     return tt::launch_status("straight_line_maps");
 }
 

@@ -836,12 +836,13 @@ trace32_batched_kernel(const __grid_constant__ GeoTable table, Ctl K, Tab T, con
 struct UniformPolicy {
     const Geo* g;
     int n;
-    mutable const Geo* cur;
     __device__ __forceinline__ const Geo& geo(long long) const { return g[0]; }
+    // asked twice per ray (start, finish): a search of the table, so that no
+    // per-lane instance state stays live across the step loop
     __device__ __forceinline__ Src src(long long r) const
     {
-        if (r < cur->ray_begin || r - cur->ray_begin >= cur->nrays) cur = g + instance_of(g, n, r);
-        return Src{cur->nodes, cur->ray_begin, cur->nrays};
+        const Geo& e = g[instance_of(g, n, r)];
+        return Src{e.nodes, e.ray_begin, e.nrays};
     }
     __device__ __forceinline__ const float4* nodes(const float4* kept) const { return kept; }
 };
@@ -853,8 +854,7 @@ trace32_uniform_kernel(const __grid_constant__ GeoTable table, Ctl K, Tab T, con
                        double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
                        int* __restrict__ status, int* __restrict__ nsteps)
 {
-    persistent_loop(UniformPolicy{table.g, table.n, table.g}, K, T, s0, np, perm, counter, sf, rf, phase, status,
-                    nsteps);
+    persistent_loop(UniformPolicy{table.g, table.n}, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps);
 }
 
 // --- ray bucketing by (instance, entry tile) ----------------------------------

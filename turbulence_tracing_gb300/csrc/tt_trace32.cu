@@ -83,6 +83,13 @@ Tab make_tab()
     return t;
 }
 
+// Resident tracer threads per SM the register budget is sized for (the
+// launch bounds give each thread 65536 / kThreadsPerSM registers).
+#ifndef TT_TRACE32_THREADS_PER_SM
+#define TT_TRACE32_THREADS_PER_SM 512
+#endif
+constexpr int kThreadsPerSM = TT_TRACE32_THREADS_PER_SM;
+
 // Geometry of one volume instance.
 struct Geo {
     const float4* nodes;
@@ -407,8 +414,12 @@ __device__ __forceinline__ bool init_ray(const Geo& G, const Src& src, const dou
     return true;
 }
 
-__device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const Ray& R, const double P0[3],
-                                           const double u0[3], long long r, long long np, double* __restrict__ sf,
+// ENTERED: the ray stepped inside the box (its state is in R); otherwise it
+// never met the box and P0, u0 hold its start (a separate instantiation, so a
+// stepping ray keeps no start state live across the step loop).
+template <bool ENTERED>
+__device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const Ray& R, const double* P0,
+                                           const double* u0, long long r, long long np, double* __restrict__ sf,
                                            double* __restrict__ rf, double* __restrict__ phase,
                                            int* __restrict__ status, int* __restrict__ nsteps)
 {
@@ -416,7 +427,7 @@ __device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const R
     // t_end for rays outside the box (zero field there): rays that left the box,
     // and rays that never meet it (whole interval).
     double P[3], u[3], ds = 0.0;
-    if (R.entered) {
+    if (ENTERED) {
         const double sig = (double)R.sig + (double)R.sigc;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -709,7 +720,6 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
     unsigned wnext = 0, wend = 0;  // the warp's chunk of perm positions (warp-uniform)
     const float4* nodes = nullptr;
     Ray R;
-    double P0[3], u0[3];
     float coef[4][8];
     R.state = 1;
     for (;;) {
@@ -748,8 +758,9 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
                     busy = true;
                     const Src src = pol.src(ray);
                     nodes = src.nodes;
+                    double P0[3], u0[3];
                     if (!init_ray(pol.geo(ray), src, s0, np, ray, R, P0, u0)) {
-                        finish_ray(pol.geo(ray), src, R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
+                        finish_ray<false>(pol.geo(ray), src, R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
                         busy = false;  // picked up again on the next pass
                     }
                 } else if (nb == ne) {
@@ -768,7 +779,8 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
         if (busy) {
             step(pol.geo(ray), pol.nodes(nodes), K, T, R, coef);
             if (R.state != 0) {
-                finish_ray(pol.geo(ray), pol.src(ray), R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
+                finish_ray<true>(pol.geo(ray), pol.src(ray), R, nullptr, nullptr, ray, np, sf, rf, phase, status,
+                                 nsteps);
                 busy = false;
             }
         }
@@ -783,7 +795,7 @@ struct SinglePolicy {
 };
 
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 512 / BLOCK)
+__global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
 trace32_kernel(const Geo G, Ctl K, Tab T, const double* __restrict__ s0, long long np,
                const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
                double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
@@ -820,7 +832,7 @@ struct MixedPolicy {
 };
 
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 512 / BLOCK)
+__global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
 trace32_batched_kernel(const __grid_constant__ GeoTable table, Ctl K, Tab T, const double* __restrict__ s0, long long np,
                        const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
                        double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
@@ -848,7 +860,7 @@ struct UniformPolicy {
 };
 
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 512 / BLOCK)
+__global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
 trace32_uniform_kernel(const __grid_constant__ GeoTable table, Ctl K, Tab T, const double* __restrict__ s0,
                        long long np, const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
                        double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,

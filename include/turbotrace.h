@@ -145,7 +145,7 @@ typedef struct tt_trace_opts {
     double atol_phase;  /* FP32 only: absolute phase tolerance (rad) */
     int64_t max_steps;  /* per-ray cap on attempted steps; 0 = TT_DEFAULT_MAX_STEPS */
     int32_t with_phase; /* integrate the phase as an extra state */
-    int32_t block_size; /* FP32 tracer: threads per block, 64, 128 or 256 (0 = 128) */
+    int32_t block_size; /* FP32 tracer: threads per block, 64, 128 or 256 (0 = 256) */
     int32_t ray_chunk;  /* FP32 tracer: consecutive (bucketed) rays a warp takes from the work
                            counter at a time, a multiple of 32 up to 1024; 0 = 32 */
 } tt_trace_opts;

@@ -16,7 +16,9 @@
 // a face is redone ending at the crossing.  Outside the box the ray is a
 // straight line, finished analytically.  Error control per ray (scipy's
 // controller constants) on position (cells), direction and phase.  Path
-// length and phase are compensated sums.
+// length and phase are compensated sums.  The interpolant and the stage
+// combinations of the two transverse components run as packed FP32x2 FMAs
+// (__ffma2_rn: per lane the same rounding as fmaf, so results are unchanged).
 //
 // Work distribution: rays are bucketed by (instance, the 4x4-cell tile they
 // start in) -- the volume's own tile order -- then a persistent grid of
@@ -45,6 +47,13 @@ struct Tab {
     float e[7];
     float ea[6];     // sum_j e_j a[j][k] with a[6] = b
     float b[6];
+    // the same coefficients duplicated into pairs, for packed FP32x2 FMAs on
+    // the two transverse components
+    float2 cs2[7];
+    float2 a2[7][6];
+    float2 aa2[7][6];
+    float2 e2[7];
+    float2 ea2[6];
 };
 
 Tab make_tab()
@@ -80,6 +89,15 @@ Tab make_tab()
         t.ea[k] = (float)acc;
         t.b[k] = (float)B[k];
     }
+    for (int s = 0; s < 7; ++s) {
+        t.cs2[s] = make_float2(t.cs[s], t.cs[s]);
+        t.e2[s] = make_float2(t.e[s], t.e[s]);
+        for (int k = 0; k < 6; ++k) {
+            t.a2[s][k] = make_float2(t.a[s][k], t.a[s][k]);
+            t.aa2[s][k] = make_float2(t.aa[s][k], t.aa[s][k]);
+        }
+    }
+    for (int k = 0; k < 6; ++k) t.ea2[k] = make_float2(t.ea[k], t.ea[k]);
     return t;
 }
 
@@ -154,6 +172,19 @@ __device__ __forceinline__ float tri(const float* c, float fa, float fb, float f
     return fmaf(fa, t3, t6);
 }
 
+// tri() on two components at once (packed FP32x2; each lane's arithmetic is tri's).
+__device__ __forceinline__ float2 tri2(const float2* c, float fa, float fb, float fc)
+{
+    const float2 A = make_float2(fa, fa), Bv = make_float2(fb, fb), Cv = make_float2(fc, fc);
+    const float2 t1 = __ffma2_rn(c[7], Cv, c[4]);
+    const float2 t2 = __ffma2_rn(c[5], Cv, c[1]);
+    const float2 t3 = __ffma2_rn(Bv, t1, t2);
+    const float2 t4 = __ffma2_rn(c[6], Cv, c[2]);
+    const float2 t5 = __ffma2_rn(c[3], Cv, c[0]);
+    const float2 t6 = __ffma2_rn(Bv, t4, t5);
+    return __ffma2_rn(A, t3, t6);
+}
+
 // Polynomial coefficients of the trilinear interpolant of one component.
 __device__ __forceinline__ void poly(float v000, float v001, float v010, float v011, float v100, float v101,
                                      float v110, float v111, float* c)
@@ -169,7 +200,7 @@ __device__ __forceinline__ void poly(float v000, float v001, float v010, float v
 }
 
 __device__ __forceinline__ void load_cell(const Geo& G, const float4* __restrict__ nodes, long long tbase, int ca,
-                                          int cb, int cc, float (*coef)[8])
+                                          int cb, int cc, float2 (*coef)[8])
 {
     const int cl = cc & (G.bd - 1);
     const int dc = (cl == G.bd - 1) ? G.brick_f4 - (G.bd - 1) : 1;
@@ -180,10 +211,16 @@ __device__ __forceinline__ void load_cell(const Geo& G, const float4* __restrict
     const float4 n010 = __ldg(p + db), n011 = __ldg(p + db + dc);
     const float4 n100 = __ldg(p + da), n101 = __ldg(p + da + dc);
     const float4 n110 = __ldg(p + da + db), n111 = __ldg(p + da + db + dc);
-    poly(n000.x, n001.x, n010.x, n011.x, n100.x, n101.x, n110.x, n111.x, coef[0]);
-    poly(n000.y, n001.y, n010.y, n011.y, n100.y, n101.y, n110.y, n111.y, coef[1]);
-    poly(n000.z, n001.z, n010.z, n011.z, n100.z, n101.z, n110.z, n111.z, coef[2]);
-    poly(n000.w, n001.w, n010.w, n011.w, n100.w, n101.w, n110.w, n111.w, coef[3]);
+    float cx[8], cy[8], cz[8], cw[8];
+    poly(n000.x, n001.x, n010.x, n011.x, n100.x, n101.x, n110.x, n111.x, cx);
+    poly(n000.y, n001.y, n010.y, n011.y, n100.y, n101.y, n110.y, n111.y, cy);
+    poly(n000.z, n001.z, n010.z, n011.z, n100.z, n101.z, n110.z, n111.z, cz);
+    poly(n000.w, n001.w, n010.w, n011.w, n100.w, n101.w, n110.w, n111.w, cw);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        coef[0][i] = make_float2(cx[i], cy[i]);
+        coef[1][i] = make_float2(cz[i], cw[i]);
+    }
 }
 
 __device__ __forceinline__ float nm1f(float q)
@@ -478,7 +515,7 @@ __device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const R
 // the current cell's polynomial while Ps stays within kTolE of it (never past
 // a box face), the exact lookup otherwise.
 __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, const Ray& R,
-                                           const float (*coef)[8], const float Ps[3], float H[3], float& q)
+                                           const float2 (*coef)[8], const float Ps[3], float H[3], float& q)
 {
     bool home = true;
 #pragma unroll
@@ -488,10 +525,12 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restric
         home = home && Ps[a] >= lo && Ps[a] <= hi;
     }
     if (home) {
-        H[0] = tri(coef[0], Ps[0], Ps[1], Ps[2]);
-        H[1] = tri(coef[1], Ps[0], Ps[1], Ps[2]);
-        H[2] = tri(coef[2], Ps[0], Ps[1], Ps[2]);
-        q = K.with_phase ? tri(coef[3], Ps[0], Ps[1], Ps[2]) : 0.f;
+        const float2 hab = tri2(coef[0], Ps[0], Ps[1], Ps[2]);
+        const float2 hcq = tri2(coef[1], Ps[0], Ps[1], Ps[2]);
+        H[0] = hab.x;
+        H[1] = hab.y;
+        H[2] = hcq.x;
+        q = K.with_phase ? hcq.y : 0.f;
     } else {
         const float4 r = eval_exact(nodes, G.n[0], G.n[1], G.n[2], G.st_b, G.tile_f4, G.bd, G.bd_shift,
                                     G.brick_f4, R.ci[0], R.ci[1], R.ci[2], Ps[0], Ps[1], Ps[2]);
@@ -504,7 +543,7 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restric
 
 // One attempted step.  Returns with R updated.
 __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, const Tab& T, Ray& R,
-                                     float (*coef)[8])
+                                     float2 (*coef)[8])
 {
     if (R.cell_dirty) {
         const int ta = R.ci[0] >> 2, tb = R.ci[1] >> 2;
@@ -564,11 +603,30 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         phb = T.b[0] * dph;
         phe = T.e[0] * dph;
     }
+    const float2 h2 = make_float2(h, h);
+    const float2 hr2 = make_float2(h * G.r[0], h * G.r[1]);
+    const float2 u2v = make_float2(R.u[0], R.u[1]);
+    const float2 fr2 = make_float2(R.fr[0], R.fr[1]);
 #pragma unroll
     for (int s = 1; s < 7; ++s) {
         float Ps[3], us[3];
+        {  // transverse pair (components 0, 1): packed FP32x2, lane-wise the scalar arithmetic below
+            float2 sa = make_float2(0.f, 0.f), saa = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
+            for (int k = 0; k < s && k < 6; ++k) {
+                const float2 hk = make_float2(Hs[k][0], Hs[k][1]);
+                sa = __ffma2_rn(T.a2[s][k], hk, sa);
+                saa = __ffma2_rn(T.aa2[s][k], hk, saa);
+            }
+            const float2 uu = __ffma2_rn(h2, sa, u2v);
+            const float2 pp = __ffma2_rn(hr2, __ffma2_rn(T.cs2[s], u2v, __fmul2_rn(h2, saa)), fr2);
+            us[0] = uu.x;
+            us[1] = uu.y;
+            Ps[0] = pp.x;
+            Ps[1] = pp.y;
+        }
+        {
+            const int c = 2;
             float sa = 0.f, saa = 0.f;
 #pragma unroll
             for (int k = 0; k < s && k < 6; ++k) {
@@ -720,7 +778,7 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
     unsigned wnext = 0, wend = 0;  // the warp's chunk of perm positions (warp-uniform)
     const float4* nodes = nullptr;
     Ray R;
-    float coef[4][8];
+    float2 coef[2][8];
     R.state = 1;
     for (;;) {
         const bool need = !busy && !drained;
@@ -1093,18 +1151,19 @@ int run(const GeoTable& table, int nbins, const Ctl& K, int block, const double*
 #define TT_LAUNCH_UNIFORM(BS, SLOT)                                                                   \
     trace32_uniform_kernel<BS><<<occupancy_grid(trace32_uniform_kernel<BS>, BS, SLOT), BS, 0, s>>>(  \
         table, Kc, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
+    // block 0 = 256 (measured fastest on the 256^3 and 512^3 workloads)
     if (table.n == 1) {
         if (block == 64) TT_LAUNCH_SINGLE(64, 0);
-        else if (block == 256) TT_LAUNCH_SINGLE(256, 2);
-        else TT_LAUNCH_SINGLE(128, 1);
+        else if (block == 128) TT_LAUNCH_SINGLE(128, 1);
+        else TT_LAUNCH_SINGLE(256, 2);
     } else if (same_shape(table)) {
         if (block == 64) TT_LAUNCH_UNIFORM(64, 6);
-        else if (block == 256) TT_LAUNCH_UNIFORM(256, 8);
-        else TT_LAUNCH_UNIFORM(128, 7);
+        else if (block == 128) TT_LAUNCH_UNIFORM(128, 7);
+        else TT_LAUNCH_UNIFORM(256, 8);
     } else {
         if (block == 64) TT_LAUNCH_BATCH(64, 3);
-        else if (block == 256) TT_LAUNCH_BATCH(256, 5);
-        else TT_LAUNCH_BATCH(128, 4);
+        else if (block == 128) TT_LAUNCH_BATCH(128, 4);
+        else TT_LAUNCH_BATCH(256, 5);
     }
 #undef TT_LAUNCH_SINGLE
 #undef TT_LAUNCH_BATCH

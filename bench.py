@@ -40,7 +40,7 @@ ALG_BYTES_PHASE = 768  # 6 stages x 8 corners x 4 components x 4 B per ray-step 
 # one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum; the
 # command and figures are in profiles/trace32_grf512_1e7rays_dram.md).  Other
 # workloads scale it by accepted ray-steps, which is stated in the output.
-TRAFFIC_CAPTURE = {"workload": "grf512_1e+07rays_phase_3det1024", "read_bytes": 15.59e9, "write_bytes": 5.34e9,
+TRAFFIC_CAPTURE = {"workload": "grf512_1e+07rays_phase_3det1024", "read_bytes": 20.44e9, "write_bytes": 5.84e9,
                    "ray_steps": 4225486610}
 
 
@@ -283,7 +283,7 @@ def run_ours(a):
                                else "ncu capture of %s scaled by ray-steps" % TRAFFIC_CAPTURE["workload"]),
             "note": "algorithmic bytes = 768 B per ray-step (6 stages x 8 corners x 4 comps x 4 B); "
                     "a face-clamped step reads one cell's 8 nodes once and rays bucketed by entry tile "
-                    "share them in L1/L2, so DRAM traffic is ~5 B per ray-step and frac > 1 is cache reuse"}
+                    "share them in L1/L2, so DRAM traffic is ~6 B per ray-step and frac > 1 is cache reuse"}
     roof["frac"] = roof["achieved"] / peak
     roof["dram_gbs"] = roof["traffic"] / (trace_ms_avg / 1e3) / 1e9
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,

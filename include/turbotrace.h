@@ -238,6 +238,24 @@ size_t tt_grf_fft_workspace_bytes(int N);
 int tt_grf_fft(uint64_t seed, int N, const double* sqrt_p, const double* Wr, const double* Wi,
                double* out, void* workspace, size_t workspace_bytes, void* stream);
 
+/* The same construction in dim = 1, 2 or 3 dimensions: gaussian1D_FFT,
+ * gaussian2D_FFT, gaussian3D_FFT (turboGen.py:388-537).  sqrt_p on the half
+ * spectrum M^(dim-1) x (N+1); Wr, Wi (M^dim, centred) or NULL for Philox noise;
+ * out M^dim float64.  tt_grf_fft is dim = 3. */
+size_t tt_grf_fft_nd_workspace_bytes(int dim, int N);
+int tt_grf_fft_nd(uint64_t seed, int dim, int N, const double* sqrt_p, const double* Wr, const double* Wi,
+                  double* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* tt_cos_field -- replaces the mode sums of gaussian1Dcos, gaussian2Dcos and
+ * gaussian3Dcos (turboGen.py:40-385): at cell centres x_i = dx/2 + i dx,
+ *   out = sum_m amp_m sqrt(2) (sum over the 1, 2 or 4 sign patterns s of
+ *         cos(kx x + s_y ky y + s_z kz z + phase_s,m)),
+ * sign patterns (+), (+,+ / +,-) and (++,+-,-+,--) in the reference's order.
+ * k: (3, nmodes) device array (rows kx, ky, kz), phase: (4, nmodes), amp:
+ * (nmodes); out: (nx[, ny[, nz]]) float64, C-ordered. */
+int tt_cos_field(int dim, int nx, int ny, int nz, double dx, double dy, double dz, int nmodes, const double* k,
+                 const double* phase, const double* amp, double* out, void* stream);
+
 /* tt_grf_field: the band-limited field of the benchmark workloads on an n^3
  * grid of side L: complex Gaussian noise (Philox4x32-10, counter = mode index)
  * times |k|^(alpha/2) for kmin <= |k| <= kmax (rad/m), inverse real FFT,

@@ -1,7 +1,7 @@
 """Generate golden fixtures by running the reference implementation itself.
 
 Run in a checkout where the reference repository is available:
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py /root/reference [fixture names]
 It imports particle_tracking/particle_tracker.py, ray_transfer_matrix.py
 (with a stub matplotlib, which the reference imports only for plotting) and
 gaussian_fields/turboGen.py + calculate_spectrum_3d.py, runs them on small
@@ -48,7 +48,7 @@ def small_field(n, L, seed, ne0=1e24, delta=0.2):
     return np.maximum(ne0 * (1 + delta * g), 0.0), x
 
 
-def main(root):
+def main(root, only=None):
     pt, rtm, turboGen, cs3 = _import_reference(root)
     out = {}
 
@@ -182,16 +182,36 @@ def main(root):
     Wi = np.random.randn(M, M, M)
     out["grf_fft"] = dict(N=6, signal=sig, Wr=Wr, Wi=Wi)
 
+    # --- cosine-sum generators and the 1D / 2D FFT generators (turboGen.py:40-485)
+    def k53(k):
+        return k ** (-5 / 3)
+
+    tg = {}
+    np.random.seed(11)
+    tg["cos1"] = turboGen.gaussian1Dcos(1.0, 64, 50, 2 * np.pi, k53)
+    np.random.seed(12)
+    tg["cos2"] = turboGen.gaussian2Dcos(1.0, 0.8, 32, 24, 40, 2 * np.pi, k53)
+    np.random.seed(13)
+    tg["cos3"] = turboGen.gaussian3Dcos(1.0, 0.9, 0.8, 16, 12, 10, 30, 2 * np.pi, k53)
+    np.random.seed(14)
+    tg["fft1"] = turboGen.gaussian1D_FFT(20, k41)
+    np.random.seed(15)
+    tg["fft2"] = turboGen.gaussian2D_FFT(8, k41)
+    out["turbogen_more"] = tg
+
     # --- spectrum_3D_scalar (calculate_spectrum_3d.py:3-59)
     d = np.random.default_rng(5).standard_normal((11, 9, 13))
     kb, sp = cs3.spectrum_3D_scalar(d, 0.5, k_bin_num=20)
     out["spectrum"] = dict(data=d, dx=0.5, kb=kb, sp=sp)
 
     for name, arrs in out.items():
+        if only and name not in only:
+            continue
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"),
                             **{k: np.asarray(v) for k, v in arrs.items()})
     print("wrote", len(out), "fixtures")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # python make_golden.py [reference root] [fixture names to (re)write ...]
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", only=set(sys.argv[2:]) or None)

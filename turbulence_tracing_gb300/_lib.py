@@ -109,6 +109,11 @@ SIGNATURES = {
     "tt_grf_fft_workspace_bytes": (c_size, [c_int]),
     "tt_grf_fft": (c_int, [ctypes.c_uint64, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size,
                            c_void_p]),
+    "tt_grf_fft_nd_workspace_bytes": (c_size, [c_int, c_int]),
+    "tt_grf_fft_nd": (c_int, [ctypes.c_uint64, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size,
+                              c_void_p]),
+    "tt_cos_field": (c_int, [c_int, c_int, c_int, c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, c_int,
+                             c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tt_grf_field_workspace_bytes": (c_size, [c_int]),
     "tt_grf_field": (c_int, [ctypes.c_uint64, c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                              ctypes.c_double, ctypes.c_double, ctypes.c_double, c_int, c_void_p, c_void_p,

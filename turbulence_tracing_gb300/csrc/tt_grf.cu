@@ -1,7 +1,11 @@
 // K4: Gaussian random fields -- Philox4x32-10 noise, Hermitian spectral
 // shaping on the half spectrum, cuFFT complex-to-real inverse transform.
 //
-//  * tt_grf_fft   replaces turboGen.gaussian3D_FFT (gaussian_fields/turboGen.py:488-537).
+//  * tt_grf_fft   replaces turboGen.gaussian3D_FFT (gaussian_fields/turboGen.py:488-537);
+//    tt_grf_fft_nd also gaussian1D_FFT and gaussian2D_FFT (:388-485), the same
+//    construction in one and two dimensions.
+//  * tt_cos_field replaces the cosine-sum generators gaussian1Dcos, gaussian2Dcos,
+//    gaussian3Dcos (:40-385): sums of random-phase modes at cell centres.
 //  * tt_grf_field the band-limited, unit-variance field of the benchmark workloads.
 //
 // The shaping kernels write only the half spectrum (last axis 0..n/2) that a
@@ -76,30 +80,36 @@ __device__ inline void half_mode_noise(int i0, int i1, int i2, int n, int h, boo
     if (self) b = 0.0;
 }
 
-// gaussian3D_FFT spectrum: M = 2N+1, half length H = N+1.
-__global__ void shape_fft_kernel(uint64_t seed, int N, const double* __restrict__ sqrt_p,
+// gaussian{1,2,3}D_FFT spectrum: M = 2N+1 points per axis, half length H = N+1
+// on the last axis; dim < 3 leaves the leading axes of size 1 (index 0).
+__global__ void shape_fft_kernel(uint64_t seed, int dim, int N, const double* __restrict__ sqrt_p,
                                  const double* __restrict__ Wr, const double* __restrict__ Wi,
                                  cufftDoubleComplex* __restrict__ F)
 {
     const int M = 2 * N + 1, H = N + 1;
-    const long long total = (long long)M * M * H;
+    const int M1 = dim >= 2 ? M : 1, M0 = dim >= 3 ? M : 1;
+    const long long total = (long long)M0 * M1 * H;
     for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < total;
          li += (long long)gridDim.x * blockDim.x) {
         const int i2 = (int)(li % H);
         const long long r = li / H;
-        const int i1 = (int)(r % M);
-        const int i0 = (int)(r / M);
+        const int i1 = (int)(r % M1);
+        const int i0 = (int)(r / M1);
         double re, im;
         if (Wr) {
             // reference: W = (Wr + flip(Wr)) + 1j (Wi - flip(Wi)) on the centred grid;
             // standard index i sits at centred (i + N) % M, its mirror at (N - i) % M.
-            const long long c = ((long long)((i0 + N) % M) * M + (i1 + N) % M) * M + (i2 + N) % M;
-            const long long f = ((long long)((N - i0 + M) % M) * M + (N - i1 + M) % M) * M + (N - i2 + M) % M;
+            const long long c0 = dim >= 3 ? (i0 + N) % M : 0, f0 = dim >= 3 ? (N - i0 + M) % M : 0;
+            const long long c1 = dim >= 2 ? (i1 + N) % M : 0, f1 = dim >= 2 ? (N - i1 + M) % M : 0;
+            const long long c = (c0 * M1 + c1) * M + (i2 + N) % M;
+            const long long f = (f0 * M1 + f1) * M + (N - i2 + M) % M;
             re = Wr[c] + Wr[f];
             im = Wi[c] - Wi[f];
         } else {
             double a, b;
-            half_mode_noise(i0, i1, i2, M, H, i2 == 0, seed, kTagFFT, a, b);
+            // tags 'GRF0' (3D), 'GRF2' (2D), 'GRF3' (1D): one stream per dimension
+            half_mode_noise(i0, i1, i2, M, H, i2 == 0, seed, dim == 3 ? kTagFFT : kTagFFT + (uint32_t)(4 - dim),
+                            a, b);
             re = a * M_SQRT2;  // variance 2 per part, as Wr(k) + Wr(-k)
             im = b * M_SQRT2;
         }
@@ -112,6 +122,53 @@ __global__ void shape_fft_kernel(uint64_t seed, int N, const double* __restrict_
             v.y = 0.0;
         }
         F[li] = v;
+    }
+}
+
+// Cosine-sum fields (turboGen.py:40-385) at cell centres xc_i = dx/2 + i dx (and y, z):
+//   dim 1: sum_m amp_m sqrt2 cos(kx xc + p0)
+//   dim 2: sum_m amp_m sqrt2 (cos(kx xc + ky yc + p0) + cos(kx xc - ky yc + p1))
+//   dim 3: sum_m amp_m sqrt2 (cos(kx xc + ky yc + kz zc + p0) + cos(kx xc + ky yc - kz zc + p1)
+//                           + cos(kx xc - ky yc + kz zc + p2) + cos(kx xc - ky yc - kz zc + p3))
+// with the reference's operation order (explicitly rounded, no contraction).
+// k: (3, nm) wavevectors, p: (4, nm) phases, amp: (nm); out C-ordered (nx[, ny[, nz]]).
+__global__ void cos_field_kernel(int dim, int nx, int ny, int nz, double dx, double dy, double dz, int nm,
+                                 const double* __restrict__ k, const double* __restrict__ p,
+                                 const double* __restrict__ amp, double* __restrict__ out)
+{
+    const long long total = (long long)nx * ny * nz;
+    for (long long li = blockIdx.x * (long long)blockDim.x + threadIdx.x; li < total;
+         li += (long long)gridDim.x * blockDim.x) {
+        const int kk = (int)(li % nz);
+        const long long r = li / nz;
+        const int j = (int)(r % ny);
+        const int i = (int)(r / ny);
+        const double xc = __dadd_rn(dx / 2.0, __dmul_rn((double)i, dx));
+        const double yc = __dadd_rn(dy / 2.0, __dmul_rn((double)j, dy));
+        const double zc = __dadd_rn(dz / 2.0, __dmul_rn((double)kk, dz));
+        double sum = 0.0;
+        for (int m = 0; m < nm; ++m) {
+            const double ax = __dmul_rn(k[m], xc);
+            const double w = __dmul_rn(amp[m], M_SQRT2);
+            double c;
+            if (dim == 1) {
+                c = cos(__dadd_rn(ax, p[m]));
+            } else {
+                const double ay = __dmul_rn(k[nm + m], yc);
+                const double xpy = __dadd_rn(ax, ay), xmy = __dsub_rn(ax, ay);
+                if (dim == 2) {
+                    c = __dadd_rn(cos(__dadd_rn(xpy, p[m])), cos(__dadd_rn(xmy, p[nm + m])));
+                } else {
+                    const double az = __dmul_rn(k[2 * nm + m], zc);
+                    c = __dadd_rn(__dadd_rn(__dadd_rn(cos(__dadd_rn(__dadd_rn(xpy, az), p[m])),
+                                                      cos(__dadd_rn(__dsub_rn(xpy, az), p[nm + m]))),
+                                            cos(__dadd_rn(__dadd_rn(xmy, az), p[2 * nm + m]))),
+                                  cos(__dadd_rn(__dsub_rn(xmy, az), p[3 * nm + m])));
+                }
+            }
+            sum = __dadd_rn(sum, __dmul_rn(w, c));
+        }
+        out[li] = sum;
     }
 }
 
@@ -242,26 +299,33 @@ int cufft_status(cufftResult r, const char* where)
     return TT_ERR_CUFFT;
 }
 
-// Size of the Z2D work area cuFFT needs for an n^3 transform (plan made and destroyed).
-int z2d_work_bytes(int n, size_t* bytes)
+int make_z2d_plan(cufftHandle p, int dim, int n, size_t* w)
+{
+    if (dim == 1) return cufft_status(cufftMakePlan1d(p, n, CUFFT_Z2D, 1, w), "cufftMakePlan1d");
+    if (dim == 2) return cufft_status(cufftMakePlan2d(p, n, n, CUFFT_Z2D, w), "cufftMakePlan2d");
+    return cufft_status(cufftMakePlan3d(p, n, n, n, CUFFT_Z2D, w), "cufftMakePlan3d");
+}
+
+// Size of the Z2D work area cuFFT needs for an n^dim transform (plan made and destroyed).
+int z2d_work_bytes(int n, size_t* bytes, int dim = 3)
 {
     cufftHandle p;
     TT_TRY(cufft_status(cufftCreate(&p), "cufftCreate"));
     int rc = cufft_status(cufftSetAutoAllocation(p, 0), "cufftSetAutoAllocation");
     size_t w = 0;
-    if (rc == TT_OK) rc = cufft_status(cufftMakePlan3d(p, n, n, n, CUFFT_Z2D, &w), "cufftMakePlan3d");
+    if (rc == TT_OK) rc = make_z2d_plan(p, dim, n, &w);
     cufftDestroy(p);
     *bytes = w;
     return rc;
 }
 
-int run_z2d(int n, cufftDoubleComplex* in, double* out, void* work, cudaStream_t s)
+int run_z2d(int n, cufftDoubleComplex* in, double* out, void* work, cudaStream_t s, int dim = 3)
 {
     cufftHandle p;
     TT_TRY(cufft_status(cufftCreate(&p), "cufftCreate"));
     size_t w = 0;
     int rc = cufft_status(cufftSetAutoAllocation(p, 0), "cufftSetAutoAllocation");
-    if (rc == TT_OK) rc = cufft_status(cufftMakePlan3d(p, n, n, n, CUFFT_Z2D, &w), "cufftMakePlan3d");
+    if (rc == TT_OK) rc = make_z2d_plan(p, dim, n, &w);
     if (rc == TT_OK) rc = cufft_status(cufftSetWorkArea(p, work), "cufftSetWorkArea");
     if (rc == TT_OK) rc = cufft_status(cufftSetStream(p, s), "cufftSetStream");
     if (rc == TT_OK) rc = cufft_status(cufftExecZ2D(p, in, out), "cufftExecZ2D");
@@ -273,12 +337,13 @@ struct FftWs {
     size_t spec_off, work_off, total;
 };
 
-FftWs fft_ws(int N, size_t work)
+FftWs fft_ws(int N, size_t work, int dim = 3)
 {
     const long long M = 2LL * N + 1, H = N + 1;
+    const long long lead = dim == 3 ? M * M : (dim == 2 ? M : 1);
     FftWs L;
     L.spec_off = 0;
-    L.work_off = tt::align_up(sizeof(cufftDoubleComplex) * (size_t)(M * M * H), 256);
+    L.work_off = tt::align_up(sizeof(cufftDoubleComplex) * (size_t)(lead * H), 256);
     L.total = tt::align_up(L.work_off + work, 256);
     return L;
 }
@@ -302,24 +367,25 @@ FieldWs field_ws(int n, size_t work)
 
 }  // namespace
 
-extern "C" size_t tt_grf_fft_workspace_bytes(int N)
+extern "C" size_t tt_grf_fft_nd_workspace_bytes(int dim, int N)
 {
-    if (N < 1) return 0;
+    if (N < 1 || dim < 1 || dim > 3) return 0;
     size_t w = 0;
-    if (z2d_work_bytes(2 * N + 1, &w) != TT_OK) return 0;
-    return fft_ws(N, w).total;
+    if (z2d_work_bytes(2 * N + 1, &w, dim) != TT_OK) return 0;
+    return fft_ws(N, w, dim).total;
 }
 
-extern "C" int tt_grf_fft(uint64_t seed, int N, const double* sqrt_p, const double* Wr, const double* Wi, double* out,
-                          void* workspace, size_t workspace_bytes, void* stream)
+extern "C" int tt_grf_fft_nd(uint64_t seed, int dim, int N, const double* sqrt_p, const double* Wr, const double* Wi,
+                             double* out, void* workspace, size_t workspace_bytes, void* stream)
 {
+    if (dim < 1 || dim > 3) return tt::invalid("grf_fft: dim must be 1, 2 or 3");
     if (N < 1) return tt::invalid("grf_fft: N must be >= 1");
     if (!sqrt_p || !out) return tt::invalid("grf_fft: null pointer");
     if ((Wr == nullptr) != (Wi == nullptr)) return tt::invalid("grf_fft: give both Wr and Wi or neither");
     const int M = 2 * N + 1;
     size_t w = 0;
-    TT_TRY(z2d_work_bytes(M, &w));
-    const FftWs L = fft_ws(N, w);
+    TT_TRY(z2d_work_bytes(M, &w, dim));
+    const FftWs L = fft_ws(N, w, dim);
     if (!workspace || workspace_bytes < L.total) {
         tt::set_detail("grf_fft: workspace needs %zu bytes", L.total);
         return TT_ERR_WORKSPACE_TOO_SMALL;
@@ -327,13 +393,35 @@ extern "C" int tt_grf_fft(uint64_t seed, int N, const double* sqrt_p, const doub
     cudaStream_t s = tt::as_stream(stream);
     char* ws = static_cast<char*>(workspace);
     cufftDoubleComplex* F = reinterpret_cast<cufftDoubleComplex*>(ws + L.spec_off);
-    const long long nh = (long long)M * M * (N + 1);
-    shape_fft_kernel<<<grid_for(nh), 256, 0, s>>>(seed, N, sqrt_p, Wr, Wi, F);
+    const long long lead = dim == 3 ? (long long)M * M : (dim == 2 ? M : 1);
+    const long long nh = lead * (N + 1);
+    shape_fft_kernel<<<grid_for(nh), 256, 0, s>>>(seed, dim, N, sqrt_p, Wr, Wi, F);
     TT_TRY(tt::launch_status("grf_fft shaping kernel"));
-    TT_TRY(run_z2d(M, F, out, ws + L.work_off, s));
-    const long long nv = (long long)M * M * M;
+    TT_TRY(run_z2d(M, F, out, ws + L.work_off, s, dim));
+    const long long nv = lead * M;
     scale_kernel<<<grid_for(nv), 256, 0, s>>>(out, nv, 1.0 / (double)nv);
     return tt::launch_status("grf_fft scale kernel");
+}
+
+extern "C" size_t tt_grf_fft_workspace_bytes(int N) { return tt_grf_fft_nd_workspace_bytes(3, N); }
+
+extern "C" int tt_cos_field(int dim, int nx, int ny, int nz, double dx, double dy, double dz, int nmodes,
+                            const double* k, const double* phase, const double* amp, double* out, void* stream)
+{
+    if (dim < 1 || dim > 3) return tt::invalid("cos_field: dim must be 1, 2 or 3");
+    if (nx < 1 || (dim >= 2 && ny < 1) || (dim == 3 && nz < 1) || nmodes < 0) return tt::invalid("cos_field: sizes");
+    if (!k || !phase || !amp || !out) return tt::invalid("cos_field: null pointer");
+    const int Ny = dim >= 2 ? ny : 1, Nz = dim == 3 ? nz : 1;
+    const long long total = (long long)nx * Ny * Nz;
+    cos_field_kernel<<<grid_for(total), 256, 0, tt::as_stream(stream)>>>(dim, nx, Ny, Nz, dx, dy, dz, nmodes, k, phase,
+                                                                         amp, out);
+    return tt::launch_status("cos_field kernel");
+}
+
+extern "C" int tt_grf_fft(uint64_t seed, int N, const double* sqrt_p, const double* Wr, const double* Wi, double* out,
+                          void* workspace, size_t workspace_bytes, void* stream)
+{
+    return tt_grf_fft_nd(seed, 3, N, sqrt_p, Wr, Wi, out, workspace, workspace_bytes, stream);
 }
 
 extern "C" size_t tt_grf_field_workspace_bytes(int n)

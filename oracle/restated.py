@@ -412,3 +412,61 @@ def workload_density(n, L, alpha, delta, ne0, seed):
     np.maximum(ne, 0.0, out=ne)
     x = np.linspace(-L / 2, L / 2, n)
     return ne, x
+
+
+# ---------------------------------------------------------------------------
+# gaussian_fields/turboGen.py: cosine-sum generators (:40-385), vectorised
+# ---------------------------------------------------------------------------
+def gaussian_cos(dim, l, n, nmodes, wn1, especf):
+    """gaussian1Dcos / gaussian2Dcos / gaussian3Dcos with the reference's draws
+    from the global numpy state (same order), summed over modes at once."""
+    d = [li / ni for li, ni in zip(l, n)]
+    wnn = max(np.pi / di for di in d)
+    dk = (wnn - wn1) / nmodes
+    wn = wn1 + 0.5 * dk + np.arange(0, nmodes) * dk
+    dkn = np.ones(nmodes) * dk
+    espec = especf(wn).clip(0.0)
+    A = np.sqrt(2.0 * espec * dkn ** dim)
+    c = [di / 2.0 + np.arange(0, ni) * di for di, ni in zip(d, n)]
+    if dim == 1:
+        phi = 2.0 * np.pi * np.random.uniform(0.0, 1.0, nmodes)
+        np.random.uniform(0.0, 1.0, nmodes)
+        arg = wn[None, :] * c[0][:, None] + phi
+        return (A * np.sqrt(2.0) * np.cos(arg)).sum(-1)
+    if dim == 2:
+        phi, psi, theta = (2.0 * np.pi * np.random.uniform(0.0, 1.0, nmodes) for _ in range(3))
+        kx, ky = np.cos(theta) * wn, np.sin(theta) * wn
+        ax = kx * c[0][:, None, None]
+        ay = ky * c[1][None, :, None]
+        return (A * np.sqrt(2.0) * (np.cos(ax + ay + phi) + np.cos(ax - ay + psi))).sum(-1)
+    p1, p2, p3, p4, theta, phi = (2.0 * np.pi * np.random.uniform(0.0, 1.0, nmodes) for _ in range(6))
+    kx = np.sin(theta) * np.cos(phi) * wn
+    ky = np.sin(theta) * np.sin(phi) * wn
+    kz = np.cos(theta) * wn
+    ax = kx * c[0][:, None, None, None]
+    ay = ky * c[1][None, :, None, None]
+    az = kz * c[2][None, None, :, None]
+    return (A * np.sqrt(2.0) * (np.cos(ax + ay + az + p1) + np.cos(ax + ay - az + p2) +
+                                np.cos(ax - ay + az + p3) + np.cos(ax - ay - az + p4))).sum(-1)
+
+
+def gaussian_fft_nd(dim, N, k_func, Wr, Wi):
+    """gaussian1D_FFT / gaussian2D_FFT / gaussian3D_FFT (turboGen.py:388-537) for
+    given noise arrays (as the reference draws them)."""
+    M = 2 * N + 1
+    k = np.fft.fftfreq(M)
+    if dim == 1:
+        K = np.sqrt(k ** 2)
+    elif dim == 2:
+        KX, KY = np.meshgrid(k, k)
+        K = np.sqrt(KX ** 2 + KY ** 2)
+    else:
+        KX, KY, KZ = np.meshgrid(k, k, k)
+        K = np.sqrt(KX ** 2 + KY ** 2 + KZ ** 2)
+    K = np.fft.fftshift(K)
+    W = (Wr + np.flip(Wr)) + 1j * (Wi - np.flip(Wi))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        F = W * np.sqrt(k_func(K))
+    F = np.fft.ifftshift(F)
+    F[(0,) * dim] = 0
+    return np.fft.ifftn(F).real

@@ -87,3 +87,44 @@ def test_workload_field_spectrum_and_variance(cuda):
     assert abs(slope - alpha) < 0.01 * abs(alpha), slope
     keep = g > -1.0
     np.testing.assert_allclose(g[keep], g_raw[keep], rtol=1e-9, atol=1e-9)
+
+
+def test_cosine_generators_match_reference(cuda):
+    """gaussian{1,2,3}Dcos: same draws from a seeded np.random as the reference,
+    mode sums on the GPU, against the reference's own output."""
+    from tests.conftest import golden
+    from turbulence_tracing_gb300 import turboGen
+
+    g = golden("turbogen_more")
+    k53 = lambda k: k ** (-5 / 3)  # noqa: E731
+    np.random.seed(11)
+    r1 = turboGen.gaussian1Dcos(1.0, 64, 50, 2 * np.pi, k53)
+    np.random.seed(12)
+    r2 = turboGen.gaussian2Dcos(1.0, 0.8, 32, 24, 40, 2 * np.pi, k53)
+    np.random.seed(13)
+    r3 = turboGen.gaussian3Dcos(1.0, 0.9, 0.8, 16, 12, 10, 30, 2 * np.pi, k53)
+    for r, ref in ((r1, g["cos1"]), (r2, g["cos2"]), (r3, g["cos3"])):
+        assert r.shape == ref.shape
+        assert np.abs(r - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_nd_fft_generators_match_reference(cuda):
+    """gaussian1D_FFT / gaussian2D_FFT with the reference's noise arrays, and
+    with Philox noise: real, zero mean, reproducible from the seed."""
+    from tests.conftest import golden
+    from turbulence_tracing_gb300 import turboGen
+
+    g = golden("turbogen_more")
+    k41 = lambda k: k ** (-5 / 3)  # noqa: E731
+    for dim, seed, N, fn in ((1, 14, 20, turboGen.gaussian1D_FFT), (2, 15, 8, turboGen.gaussian2D_FFT)):
+        M = 2 * N + 1
+        np.random.seed(seed)
+        Wr = np.random.randn(*(M,) * dim)
+        Wi = np.random.randn(*(M,) * dim)
+        r = fn(N, k41, Wr=Wr, Wi=Wi)
+        ref = g["fft%d" % dim]
+        assert r.shape == ref.shape
+        assert np.abs(r - ref).max() <= 1e-12 * np.abs(ref).max()
+        a = fn(N, k41, seed=7)
+        b = fn(N, k41, seed=7)
+        assert np.array_equal(a, b) and abs(a.mean()) <= 1e-12 * np.abs(a).max()

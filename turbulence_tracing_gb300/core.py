@@ -376,6 +376,39 @@ def grf_fft(N, sqrt_p_half, seed=0, Wr=None, Wi=None):
     return out
 
 
+def grf_fft_nd(dim, N, sqrt_p_half, seed=0, Wr=None, Wi=None):
+    """gaussian{1,2,3}D_FFT core: sqrt_p_half (M,)*(dim-1) + (N+1,) device float64."""
+    dev = require_cuda()
+    L = _lib.lib()
+    M = 2 * N + 1
+    sp = _f64_dev(sqrt_p_half, dev)
+    if tuple(sp.shape) != (M,) * (dim - 1) + (N + 1,):
+        raise ValueError("sqrt_p_half must be (M,)*(dim-1) + (N+1,)")
+    wr = _f64_dev(Wr, dev) if Wr is not None else None
+    wi = _f64_dev(Wi, dev) if Wi is not None else None
+    out = torch.empty((M,) * dim, dtype=torch.float64, device=dev)
+    ws = workspace(L.tt_grf_fft_nd_workspace_bytes(dim, N), dev)
+    check(L.tt_grf_fft_nd(int(seed) & 0xFFFFFFFFFFFFFFFF, dim, N, _ptr(sp), _ptr(wr), _ptr(wi), _ptr(out), _ptr(ws),
+                          ws.numel(), _stream()), "tt_grf_fft_nd")
+    return out
+
+
+def cos_field(dim, n, d, k, phase, amp):
+    """Cosine-sum field at cell centres (tt_cos_field): n, d per axis (dim
+    entries), k (3, nm), phase (4, nm), amp (nm) float64."""
+    dev = require_cuda()
+    nm = int(np.asarray(amp).shape[0])
+    kt = _f64_dev(np.zeros((3, nm)) if nm == 0 else k, dev).contiguous()
+    pt = _f64_dev(np.zeros((4, nm)) if nm == 0 else phase, dev).contiguous()
+    at = _f64_dev(amp, dev).contiguous()
+    nn = list(n) + [1] * (3 - dim)
+    dd = list(d) + [1.0] * (3 - dim)
+    out = torch.empty(tuple(nn[:dim]), dtype=torch.float64, device=dev)
+    check(_lib.lib().tt_cos_field(dim, nn[0], nn[1], nn[2], float(dd[0]), float(dd[1]), float(dd[2]), nm, _ptr(kt),
+                                  _ptr(pt), _ptr(at), _ptr(out), _stream()), "tt_cos_field")
+    return out
+
+
 def philox(seed, tag, count):
     dev = require_cuda()
     out = torch.empty((4, count), dtype=torch.int32, device=dev)

@@ -84,7 +84,7 @@ def workload_config(a):
             "spectrum_exponent": a.alpha, "delta": a.delta, "ne0_m3": a.ne0, "rays": int(a.rays),
             "beam_sigma_m": a.sigma, "divergence_rad": a.div, "lwl_m": a.lwl,
             "detectors": ["shadowgraphy", "schlieren_knife_x0", "interferometry"], "detector_bins": [a.det, a.det],
-            "detector_extent_mm": 12.0, "optics_f_mm": 100.0, "aperture_mm": 25.0,
+            "detector_extent_mm": 8.0 * a.sigma * 1e3, "optics_f_mm": 100.0, "aperture_mm": 25.0,
             "fp32_tol": {"rtol": 1e-7, "atol_cells": 1e-5, "atol_phase": 1e-5}, "seed": a.seed,
             "l2": "inputs larger than L2 (density 0.5 GB, node volume 3.4 GB, rays 0.5 GB); no flush"}
 
@@ -200,7 +200,7 @@ def run_ours(a):
     s0 = torch.as_tensor(s0_host, device=dev)
 
     det = a.det
-    ext_mm = 6.0
+    ext_mm = 4.0 * a.sigma * 1e3  # +-4 beam sigma (6 mm for the default 1.5 mm beam)
     f_mm, R_mm = 100.0, 25.0
     relay = lambda mid: ([(_lib.OPTIC_M_TO_MM, 0, 0, 0), (_lib.OPTIC_DISTANCE, f_mm, 0, 0),
                           (_lib.OPTIC_CIRC_APERTURE, R_mm, 0, 0), (_lib.OPTIC_LENS, f_mm, f_mm, 0),

@@ -458,7 +458,7 @@ def surrogate_run(a):
     Xte, _, ste, truth, _ = SG.build_dataset(W, SG.draw_fields(a.sur_test, seed=a.seed + 12), keep_truth=True)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
-    net = fno.FNO(S, in_ch=SG.IN_CH, out_ch=3, layers=4, seed=a.seed)
+    net = fno.FNO(S, in_ch=W.in_ch, out_ch=3, layers=4, seed=a.seed)
     trainer = SG.Trainer(net, X, Y, batch=8)
     hist, sps = trainer.fit(a.sur_epochs, lr=1e-3)
     res = SG.evaluate(W, net, Xte, ste, truth)
@@ -482,7 +482,7 @@ def surrogate_run(a):
     torch.cuda.synchronize()
     us_fwd = e0.elapsed_time(e1) * 1e3 / 80
     C = 32
-    fwd_bytes = 4 * (6 * C * S * S * 1 + 16 * C * 32 * S) + (4 * SG.IN_CH + 2 * C) * S * S + (2 * C + 12) * S * S
+    fwd_bytes = 4 * (6 * C * S * S * 1 + 16 * C * 32 * S) + (4 * W.in_ch + 2 * C) * S * S + (2 * C + 12) * S * S
     peak, peak_kind = peaks()
     # the pipeline against tracing every held-out field
     params = SG.draw_fields(a.sur_test, seed=a.seed + 12)[half:]

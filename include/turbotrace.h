@@ -272,15 +272,16 @@ int tt_philox(uint64_t seed, uint32_t tag, int64_t count, uint32_t* out, void* s
 
 /* Straight-line path integrals through an n_e grid along z, at the centres of
  * a P x P pixel grid over the box face (pixel (i, j) at x0 + (i + 0.5)(xN - x0)/P,
- * y0 + (j + 0.5)(yN - y0)/P): out FP32 [nout][P][P], nout 3 or 5 =
+ * y0 + (j + 0.5)(yN - y0)/P): out FP32 [3 + 2 nslab][P][P] =
  *   -1/2 integral dq/dx dz, -1/2 integral dq/dy dz (straight-line deflection, rad),
  *   k0 integral (sqrt(1 - q) - 1) dz (straight-line phase, rad),
- *   and with nout = 5 the first moments -1/2 integral (z - z0)/Lz dq/dx dz and the same for y,
+ *   then for each of nslab (0..8) equal slabs of cells along z the two
+ *   deflection integrals over that slab,
  * q = min(ne / n_c, ne_max) with n_c and k0 = omega / c as calc_dndr forms them
  * (particle_tracker.py:227-232), gradients by numpy.gradient's rule, all fields
  * trilinear.  x, y, z: host arrays of uniform node coordinates. */
 int tt_straight_line_maps(const void* ne, int ne_dtype, int nx, int ny, int nz, const double* x, const double* y,
-                          const double* z, double lwl, double ne_max, int P, int nout, float* out, void* stream);
+                          const double* z, double lwl, double ne_max, int P, int nslab, float* out, void* stream);
 
 /* Geometric-optics shadowgram of a deflection map theta FP32 [2][P][P] (angles
  * of rays leaving the centres of a P x P pixel grid of pitch `pitch` m):
@@ -308,7 +309,7 @@ int tt_shadowgram(const float* theta, int P, double pitch, double D, float* inte
 #define TT_FNO_WIDTH 32
 #define TT_FNO_MODES 16
 #define TT_FNO_MAX_LAYERS 8
-#define TT_FNO_MAX_IN 8
+#define TT_FNO_MAX_IN 16
 #define TT_FNO_MAX_OUT 4
 
 typedef struct tt_fno_dims {

@@ -35,11 +35,14 @@ def test_straight_line_maps_match_restatement(cuda):
     from turbulence_tracing_gb300 import core
 
     ne, x = R.workload_density(40, 1e-3, -3.0, 0.2, 5e24, 3)
-    m = core.straight_line_maps(ne, x, x, x, 32, lwl=1064e-9, moments=True).cpu().numpy()
+    m = core.straight_line_maps(ne, x, x, x, 32, lwl=1064e-9, nslab=3).cpu().numpy()
     ax, ay = _maps_restated(ne, x, 1064e-9, 32)
     scale = np.abs(ax).max()
     assert np.abs(m[0] - ax).max() <= 1e-5 * scale
     assert np.abs(m[1] - ay).max() <= 1e-5 * scale
+    # the slab integrals add up to the whole path
+    assert np.abs(m[3::2].sum(0) - m[0]).max() <= 1e-5 * scale
+    assert np.abs(m[4::2].sum(0) - m[1]).max() <= 1e-5 * scale
 
 
 def test_straight_line_map_is_first_order_trace(cuda):
@@ -65,7 +68,7 @@ def test_trained_surrogate_beats_straight_line_and_fallback_bounds_error(cuda):
     W = SG.Workload(128)
     Xtr, Ytr, _, _, _ = SG.build_dataset(W, SG.draw_fields(384, seed=1))
     Xte, _, ste, truth, _ = SG.build_dataset(W, SG.draw_fields(48, seed=2), keep_truth=True)
-    net = fno.FNO(128, in_ch=SG.IN_CH, out_ch=3, layers=4, seed=0)
+    net = fno.FNO(128, in_ch=W.in_ch, out_ch=3, layers=4, seed=0)
     hist, _ = SG.Trainer(net, Xtr, Ytr, batch=8).fit(12, lr=1e-3)
     assert hist[-1] < 0.7 * hist[0], hist
     res = SG.evaluate(W, net, Xte, ste, truth)

@@ -65,7 +65,7 @@ class TTFnoDims(ctypes.Structure):
 FNO_WIDTH = 32
 FNO_MODES = 16
 FNO_MAX_LAYERS = 8
-FNO_MAX_IN = 8
+FNO_MAX_IN = 16
 FNO_MAX_OUT = 4
 
 

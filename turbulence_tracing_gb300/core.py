@@ -310,21 +310,21 @@ def detect(rf, ops, nbx=1, nby=1, xr=(-1.0, 1.0), yr=(-1.0, 1.0), weights=None, 
 # ---------------------------------------------------------------------------
 # K4
 # ---------------------------------------------------------------------------
-def straight_line_maps(ne, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, moments=False):
-    """(3, P, P) float32: straight-line deflection angles (x, y) and phase at
-    the centres of a P x P pixel grid over the z = z0 face (tt_straight_line_maps);
-    with moments=True (5, P, P), adding the first z-moments of the deflection."""
+def straight_line_maps(ne, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, nslab=0):
+    """(3 + 2 nslab, P, P) float32: straight-line deflection angles (x, y) and
+    phase at the centres of a P x P pixel grid over the z = z0 face, then the
+    deflection over each of nslab slabs along z (tt_straight_line_maps)."""
     dev = require_cuda()
     ne_t = _dens_dev(ne, dev)
     nx, ny, nz = ne_t.shape
     xa, ya, za = (np.ascontiguousarray(np.asarray(c, dtype=np.float64)) for c in (x, y, z))
-    nout = 5 if moments else 3
+    nout = 3 + 2 * int(nslab)
     if out is None:
         out = torch.empty((nout, P, P), dtype=torch.float32, device=dev)
     dp = ctypes.POINTER(ctypes.c_double)
     check(_lib.lib().tt_straight_line_maps(_ptr(ne_t), _dtype_code(ne_t), nx, ny, nz, xa.ctypes.data_as(dp),
                                            ya.ctypes.data_as(dp), za.ctypes.data_as(dp), float(lwl), float(ne_max),
-                                           int(P), nout, _ptr(out), _stream()), "tt_straight_line_maps")
+                                           int(P), int(nslab), _ptr(out), _stream()), "tt_straight_line_maps")
     return out
 
 

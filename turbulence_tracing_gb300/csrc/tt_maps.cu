@@ -7,8 +7,8 @@
 //   out[0] = -1/2 * integral dq/dx dz      (paraxial deflection angle, rad)
 //   out[1] = -1/2 * integral dq/dy dz
 //   out[2] = k0 * integral (sqrt(1 - q) - 1) dz   (phase, rad; k0 = omega / c)
-//   out[3] = -1/2 * integral (z - z0) / Lz dq/dx dz  (first moments along the path:
-//   out[4] = -1/2 * integral (z - z0) / Lz dq/dy dz   where along z the deflection builds up)
+//   out[3 + 2s], out[4 + 2s] = the two deflection integrals over slab s of nslab
+//   equal slabs of cells along z (where along the path the deflection builds up)
 // with q = min(ne / n_c, ne_max) and its gradient taken with numpy.gradient's
 // rule on the node grid (central inside, one-sided at the faces), both
 // interpolated trilinearly -- the same fields the tracer integrates.  The
@@ -18,12 +18,14 @@
 
 namespace {
 
+constexpr int kMaxSlab = 8;
+
 // One warp per pixel: lane l handles nodes k = l, l + 32, ... along z, so
 // the column reads (z is the fastest axis of the density) are coalesced; the
 // per-lane sums are combined with shuffles.
 template <typename T>
 __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, double hx, double hy, double hz,
-                            float inv_nc, float ne_max, double k0, int P, int nout, float* __restrict__ out)
+                            float inv_nc, float ne_max, double k0, int P, int nslab, float* __restrict__ out)
 {
     const int n = P * P;
     const int warp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
@@ -53,7 +55,10 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
         const float v = (float)c[k] * inv_nc;
         return v < ne_max ? v : ne_max;
     };
-    float sx = 0.f, sy = 0.f, mx = 0.f, my = 0.f, sp = 0.f;
+    float sx = 0.f, sy = 0.f, sp = 0.f;
+    float slx[kMaxSlab], sly[kMaxSlab];
+#pragma unroll
+    for (int q = 0; q < kMaxSlab; ++q) slx[q] = sly[q] = 0.f;
     for (int k = lane; k < nz; k += 32) {
         const float q00 = q(c00, k), q10 = q(c10, k), q01 = q(c01, k), q11 = q(c11, k);
         // d/dx at (ix, .) uses (ix+1) - (ix-1) (or the one-sided pair), at (ix+1, .) uses (ix+2) - ix
@@ -64,11 +69,19 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
         const float gxk = w00 * gx0 + w10 * gx1 + w01 * gx2 + w11 * gx3;
         const float gyk = w00 * gy0 + w10 * gy1 + w01 * gy2 + w11 * gy3;
         const float wz = (k == 0 || k == nz - 1) ? 0.5f : 1.f;
-        const float zr = (float)k / (float)(nz - 1);
         sx = fmaf(wz, gxk, sx);
         sy = fmaf(wz, gyk, sy);
-        mx = fmaf(wz * zr, gxk, mx);
-        my = fmaf(wz * zr, gyk, my);
+        // node k's trapezoid weight is half from cell k-1 and half from cell k,
+        // each credited to that cell's slab
+        if (nslab > 0) {
+#pragma unroll
+            for (int q = 0; q < kMaxSlab; ++q) {
+                const float wl = (k > 0 && (int)((long long)(k - 1) * nslab / (nz - 1)) == q) ? 0.5f : 0.f;
+                const float wr = (k < nz - 1 && (int)((long long)k * nslab / (nz - 1)) == q) ? 0.5f : 0.f;
+                slx[q] = fmaf(wl + wr, gxk, slx[q]);
+                sly[q] = fmaf(wl + wr, gyk, sly[q]);
+            }
+        }
         if (k + 1 < nz) {  // the cell [k, k+1]: 4-point Gauss-Legendre on the linear q(z)
             const float qk = w00 * q00 + w10 * q10 + w01 * q01 + w11 * q11;
             const float qn = w00 * q(c00, k + 1) + w10 * q(c10, k + 1) + w01 * q(c01, k + 1) + w11 * q(c11, k + 1);
@@ -85,17 +98,25 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
     for (int off = 16; off > 0; off >>= 1) {
         sx += __shfl_xor_sync(0xffffffffu, sx, off);
         sy += __shfl_xor_sync(0xffffffffu, sy, off);
-        mx += __shfl_xor_sync(0xffffffffu, mx, off);
-        my += __shfl_xor_sync(0xffffffffu, my, off);
+#pragma unroll
+        for (int q = 0; q < kMaxSlab; ++q) {
+            if (q < nslab) {
+                slx[q] += __shfl_xor_sync(0xffffffffu, slx[q], off);
+                sly[q] += __shfl_xor_sync(0xffffffffu, sly[q], off);
+            }
+        }
         sp += __shfl_xor_sync(0xffffffffu, sp, off);
     }
     if (lane == 0) {
         out[warp] = (float)(-0.5 * (double)sx * hz / hx);
         out[n + warp] = (float)(-0.5 * (double)sy * hz / hy);
         out[2 * n + warp] = (float)(k0 * (double)sp * hz);
-        if (nout > 3) {
-            out[3 * n + warp] = (float)(-0.5 * (double)mx * hz / hx);
-            out[4 * n + warp] = (float)(-0.5 * (double)my * hz / hy);
+#pragma unroll
+        for (int q = 0; q < kMaxSlab; ++q) {
+            if (q < nslab) {
+                out[(3 + 2 * q) * n + warp] = (float)(-0.5 * (double)slx[q] * hz / hx);
+                out[(4 + 2 * q) * n + warp] = (float)(-0.5 * (double)sly[q] * hz / hy);
+            }
         }
     }
 }
@@ -103,10 +124,10 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
 }  // namespace
 
 extern "C" int tt_straight_line_maps(const void* ne, int ne_dtype, int nx, int ny, int nz, const double* x,
-                                     const double* y, const double* z, double lwl, double ne_max, int P, int nout,
+                                     const double* y, const double* z, double lwl, double ne_max, int P, int nslab,
                                      float* out, void* stream)
 {
-    if (nout != 3 && nout != 5) return tt::invalid("straight_line_maps: nout must be 3 or 5");
+    if (nslab < 0 || nslab > kMaxSlab) return tt::invalid("straight_line_maps: nslab must be 0..8");
     if (!ne || !x || !y || !z || !out) return tt::invalid("straight_line_maps: NULL pointer");
     if (nx < 2 || ny < 2 || nz < 2 || P < 1) return tt::invalid("straight_line_maps: bad sizes");
     if (ne_dtype != TT_F32 && ne_dtype != TT_F64) return tt::invalid("straight_line_maps: ne_dtype");
@@ -122,10 +143,10 @@ extern "C" int tt_straight_line_maps(const void* ne, int ne_dtype, int nx, int n
     cudaStream_t s = tt::as_stream(stream);
     if (ne_dtype == TT_F32)
         maps_kernel<float><<<grid, 256, 0, s>>>((const float*)ne, nx, ny, nz, hx, hy, hz, (float)(1.0 / nc),
-                                                (float)ne_max, k0, P, nout, out);
+                                                (float)ne_max, k0, P, nslab, out);
     else
         maps_kernel<double><<<grid, 256, 0, s>>>((const double*)ne, nx, ny, nz, hx, hy, hz, (float)(1.0 / nc),
-                                                 (float)ne_max, k0, P, nout, out);
+                                                 (float)ne_max, k0, P, nslab, out);
     return tt::launch_status("straight_line_maps");
 }
 

@@ -6,13 +6,14 @@ and its phase -- and fall back to the exact FP32 tracer where the network's
 own error estimate says the prediction would miss.
 
 Per realisation (an S^3 field of side L, drawn like the batched ensemble):
-  maps     tt_straight_line_maps: straight-line deflection (2 maps), phase and
-           first z-moments of the deflection (2 maps) of the S x S
-           pixel-centre rays; the deflection and phase maps are the method
-           without the network
-  inputs   the four deflection maps / s, s the rms of the deflection, and a
-           constant map log10(s (S - 1)) -- the straight-line drift across the
-           box in cells, i.e. how far into the nonlinear regime the field is
+  maps     tt_straight_line_maps: straight-line deflection (2 maps) and phase
+           of the S x S pixel-centre rays -- the method without the network --
+           and the deflection accumulated in each of nslab slabs along the
+           path (2 maps per slab)
+  inputs   the deflection maps (total and per slab) / s, s the rms of the
+           total deflection, and a constant map log10(s (S - 1)) -- the
+           straight-line drift across the box in cells, i.e. how far into the
+           nonlinear regime the field is
   targets  (full-trace deflection - straight-line deflection) / (s^2 (S - 1))
            and (full-trace phase - straight-line phase) / (k0 L s^2): both
            corrections are second order in the field, so these are O(1)
@@ -47,9 +48,12 @@ def draw_fields(n, seed=0, exponents=(-5.0 / 3.0, -3.0, -11.0 / 3.0), delta=(0.0
 class Workload:
     """Fields, straight-line maps, exact traces and shadowgrams at one grid size."""
 
-    def __init__(self, S, L=2e-3, lwl=1064e-9, rtol=1e-7, contrast=0.2):
+    def __init__(self, S, L=2e-3, lwl=1064e-9, rtol=1e-7, contrast=0.2, nslab=4):
         self.dev = core.require_cuda()
         self.S, self.L, self.lwl, self.rtol, self.contrast = S, L, lwl, rtol, contrast
+        self.nslab = nslab
+        self.in_ch = in_channels(nslab)
+        self.n_maps = 3 + 2 * nslab
         self.x = np.linspace(-L / 2, L / 2, S)
         self.ext = float(self.x.max())
         self.t_end = float(np.linspace(0.0, math.sqrt(8.0) * self.ext / C_LIGHT, 2)[-1])
@@ -68,7 +72,7 @@ class Workload:
         return core.grf_field(self.S, self.L, p["alpha"], p["ne0"], p["delta"], p["seed"], dtype=torch.float32)
 
     def maps(self, ne, out=None):
-        return core.straight_line_maps(ne, self.x, self.x, self.x, self.S, lwl=self.lwl, out=out, moments=True)
+        return core.straight_line_maps(ne, self.x, self.x, self.x, self.S, lwl=self.lwl, out=out, nslab=self.nslab)
 
     def trace(self, ne):
         """Exact FP32 trace of the pixel-centre rays: (theta (2,S,S) f32, phase (S,S) f64, steps tensor)."""
@@ -92,16 +96,19 @@ class Workload:
         return core.shadowgram(theta.contiguous(), self.pitch, float(D))[0]
 
 
-IN_CH = 5
+def in_channels(nslab):
+    return 3 + 2 * nslab
 
 
 def encode(maps, S):
-    """Network input (5, S, S) and the scale s from straight-line maps (5, S, S)."""
+    """Network input (3 + 2 nslab, S, S) and the scale s from straight-line maps
+    (3 + 2 nslab, S, S): total and slab deflections / s, then log10 drift."""
+    nin = maps.shape[0]
     s = torch.sqrt((maps[0:2].double() ** 2).mean()).float().clamp_min(1e-30)
-    inp = torch.empty((IN_CH, S, S), dtype=torch.float32, device=maps.device)
+    inp = torch.empty((nin, S, S), dtype=torch.float32, device=maps.device)
     inp[0:2] = maps[0:2] / s
-    inp[2:4] = maps[3:5] / s
-    inp[4] = torch.log10(s * (S - 1))
+    inp[2:nin - 1] = maps[3:nin] / s
+    inp[nin - 1] = torch.log10(s * (S - 1))
     return inp, s
 
 
@@ -129,12 +136,12 @@ def build_dataset(W, params, keep_truth=False):
     """Inputs and targets (N, 3, S, S) on the device; optionally the straight-line
     maps, exact deflections and phases for evaluation."""
     N, S = len(params), W.S
-    X = torch.empty((N, IN_CH, S, S), dtype=torch.float32, device=W.dev)
+    X = torch.empty((N, W.in_ch, S, S), dtype=torch.float32, device=W.dev)
     Y = torch.empty((N, 3, S, S), dtype=torch.float32, device=W.dev)
     scale = torch.empty(N, dtype=torch.float32, device=W.dev)
     truth = None
     if keep_truth:
-        truth = {"maps": torch.empty((N, 5, S, S), dtype=torch.float32, device=W.dev), "theta": torch.empty((N, 2, S, S), dtype=torch.float32, device=W.dev),
+        truth = {"maps": torch.empty((N, W.n_maps, S, S), dtype=torch.float32, device=W.dev), "theta": torch.empty((N, 2, S, S), dtype=torch.float32, device=W.dev),
                  "phase": torch.empty((N, S, S), dtype=torch.float64, device=W.dev)}
     steps = torch.zeros((), dtype=torch.int64, device=W.dev)
     for i, p in enumerate(params):
@@ -243,7 +250,7 @@ def evaluate(W, net, X, scale, truth, batch=8):
                     "theta_err_net": rel_l2(th_net, truth["theta"][i]),
                     "phase_corr_err_net": float(torch.linalg.norm(ph_net - truth["phase"][i]) /
                                                 torch.linalg.norm(truth["phase"][i] - m[2].double())),
-                    "log_drift": float(X[i, IN_CH - 1, 0, 0])})
+                    "log_drift": float(X[i, -1, 0, 0])})
     return res
 
 
@@ -260,9 +267,9 @@ class Pipeline:
     def __init__(self, W, net, kappa, tol=0.02, batch=8):
         self.W, self.net, self.kappa, self.tol, self.B = W, net, kappa, tol, batch
         S = W.S
-        self.X = torch.empty((batch, IN_CH, S, S), dtype=torch.float32, device=W.dev)
+        self.X = torch.empty((batch, W.in_ch, S, S), dtype=torch.float32, device=W.dev)
         self.out = torch.empty((batch, 3, S, S), dtype=torch.float32, device=W.dev)
-        self.maps = torch.empty((batch, 5, S, S), dtype=torch.float32, device=W.dev)
+        self.maps = torch.empty((batch, W.n_maps, S, S), dtype=torch.float32, device=W.dev)
 
     def run(self, fields):
         """fields: list of density tensors.  Returns (intensity list, fell_back list)."""

@@ -568,7 +568,7 @@ def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
         sec = float(t.item())
     Np = s0_host.shape[1]
     h2d = Np * 6 * 8 + 3 * Np * 4 * 8 + Np * 8          # s0; rf re-uploaded by each diagnostic; phase weights
-    d2h = Np * (6 + 4 + 1) * 8 + Np * 2 * 4 + 3 * det * det * 8 + 3 * 4 * Np * 8
+    d2h = Np * (6 + 4 + 1) * 8 + Np * 2 * 4 + 4 * det * det * 8  # sf, rf, phase; status, steps; 3 H + 1 Hw
     return {"value": (tot / k) * ws / sec, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "seconds_per_step": sec, "steps": k,
             "path": "ElectronCube.solve(precision='fp32', phase=True) + Shadowgraphy, Schlieren_KE, "

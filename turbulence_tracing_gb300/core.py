@@ -58,6 +58,18 @@ def _dtype_code(t):
     return _lib.TT_F32 if t.dtype == torch.float32 else _lib.TT_F64
 
 
+def to_host(t):
+    """Device tensor -> numpy array through a pinned staging buffer (torch's
+    caching host allocator), so large results come back at the host link's
+    speed rather than through pageable copies.  Each call returns fresh memory."""
+    if t.numel() * t.element_size() < (1 << 20):
+        return t.cpu().numpy()
+    h = torch.empty(tuple(t.shape), dtype=t.dtype, device="cpu", pin_memory=True)
+    h.copy_(t, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    return h.numpy()
+
+
 def workspace(nbytes, dev):
     return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=dev)
 

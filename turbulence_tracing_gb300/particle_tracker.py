@@ -203,7 +203,7 @@ class ElectronCube:
         torch.cuda.current_stream().synchronize()
         finish = time()
         print("Ray trace completed in:\t", finish - start, "s")
-        conv = (lambda t_: t_) if on_device else (lambda t_: t_.cpu().numpy())
+        conv = (lambda t_: t_) if on_device else core.to_host
         self.sf = conv(out["sf"])
         self.rf = conv(out["rf"])
         self.status = conv(out["status"])

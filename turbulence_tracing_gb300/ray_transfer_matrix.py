@@ -147,7 +147,7 @@ class Rays:
     def rf(self):
         if self._rf is None and self._ops is not None and self._r0_m is not None:
             _, _, out = core.detect(self._r0_m, self._chain(), r_out=True, histogram=False)
-            self._rf = out if _is_t(self._r0_m) else out.cpu().numpy()
+            self._rf = out if _is_t(self._r0_m) else core.to_host(out)
         return self._rf
 
     @rf.setter
@@ -163,14 +163,12 @@ class Rays:
         nbx, nby = pix_x // bin_scale, pix_y // bin_scale
         xr = (-self.Lx / 2, self.Lx / 2)
         yr = (-self.Ly / 2, self.Ly / 2)
-        H, Hw, out = core.detect(self._r0_m, self._chain(), nbx, nby, xr, yr, weights=weights,
-                                 r_out=self._rf is None)
-        if out is not None:
-            self._rf = out if _is_t(self._r0_m) else out.cpu().numpy()
+        # the detector-plane rays (self.rf) are computed when first read, not here
+        H, Hw, _ = core.detect(self._r0_m, self._chain(), nbx, nby, xr, yr, weights=weights)
         on_dev = _is_t(self._r0_m)
-        self.H = H if on_dev else H.cpu().numpy()
+        self.H = H if on_dev else core.to_host(H)
         if Hw is not None:
-            self.Hw = Hw if on_dev else Hw.cpu().numpy()
+            self.Hw = Hw if on_dev else core.to_host(Hw)
         self.xedges = np.linspace(xr[0], xr[1], nbx + 1)
         self.yedges = np.linspace(yr[0], yr[1], nby + 1)
         if clear_mem:

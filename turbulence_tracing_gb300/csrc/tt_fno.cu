@@ -381,6 +381,9 @@ __global__ void __launch_bounds__(128) fno_wgrad_kernel(int B, const bf16* __res
     const uint32_t idesc = U::idesc_bf16(128, 128);
     uint32_t phase[2] = {0u, 0u};
     bool pending[2] = {false, false};
+    // a thread's staged rows of dz always fall on two channels (one per parity
+    // of the staging iteration): db is summed in two registers, not atomics
+    float dba[2] = {0.f, 0.f};
 
     for (long long ch = c_begin; ch < c_end; ++ch) {
         const int s = (int)((ch - c_begin) & 1);
@@ -398,8 +401,9 @@ __global__ void __launch_bounds__(128) fno_wgrad_kernel(int B, const bf16* __res
         const long long b = ch / CPS, p0 = (ch % CPS) * 256;
         uint8_t* sA = sm + s * 2 * TILE;
         uint8_t* sB = sA + TILE;
-#pragma unroll 4
-        for (int q = tid; q < 128 * 8; q += 128) {
+#pragma unroll
+        for (int it = 0; it < 8; ++it) {
+            const int q = it * 128 + tid;
             const int r8 = q & 7, kg = (q >> 3) & 7, rg = q >> 6;
             const int r = rg * 8 + r8, sl = r >> 5, ch_ = r & 31;
             const size_t g = ((size_t)b * W + ch_) * PIX + p0 + sl * 64 + kg * 8;
@@ -411,8 +415,7 @@ __global__ void __launch_bounds__(128) fno_wgrad_kernel(int B, const bf16* __res
             float sum = 0.f;
 #pragma unroll
             for (int i = 0; i < 8; ++i) sum += __bfloat162float(e[i]);
-            // rows r8 of this thread repeat with period 8 in q; channel = r & 31
-            atomicAdd(&sdb[ch_], sum);
+            dba[it & 1] += sum;  // channel ((tid >> 6) + 2 * (it & 1)) * 8 + (tid & 7)
         }
         U::fence_proxy_async();
         __syncthreads();
@@ -438,14 +441,29 @@ __global__ void __launch_bounds__(128) fno_wgrad_kernel(int B, const bf16* __res
             phase[s] ^= 1u;
         }
     }
+#pragma unroll
+    for (int p = 0; p < 2; ++p) atomicAdd(&sdb[(((tid >> 6) + 2 * p) & 3) * 8 + (tid & 7)], dba[p]);
     __syncthreads();
     if (!*abort_flag) {
         U::fence_after();
         float acc[32];
         // warp q reads TMEM lanes (q, o = lane), columns of block q: dW partial for slice q
         U::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(warp * 32), acc);
-#pragma unroll 8
-        for (int c = 0; c < W; ++c) atomicAdd(&dW[lane * W + c], acc[c]);
+        // sum the four slice partials in shared memory (the operand stages are
+        // free now; rows padded to 33 floats), then one coalesced atomic per
+        // element of dW from this block
+        float* part = reinterpret_cast<float*>(sm);
+#pragma unroll
+        for (int c = 0; c < W; ++c) part[(warp * W + lane) * (W + 1) + c] = acc[c];
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < W * W / 128; ++i) {
+            const int a = tid + 128 * i, o = a / W, c = a % W;
+            float tot = 0.f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) tot += part[(q * W + o) * (W + 1) + c];
+            atomicAdd(&dW[a], tot);
+        }
         if (tid < W) atomicAdd(&db[tid], sdb[tid]);
     }
     U::fence_before();

@@ -439,16 +439,17 @@ def batched_run(a):
 
 
 def surrogate_run(a):
-    """The learned surrogate (straight-line maps -> full-trace deflection and
-    phase correction) at a.sur_size^2 on fields drawn as the batched workload
-    at that grid: data made by the tracer itself, FNO training by the
+    """The learned surrogate (straight-line and marched maps -> full-trace
+    deflection and phase) at a.sur_size^2 on fields drawn as the batched
+    workload at that grid: data made by the tracer itself, FNO training by the
     library's kernels, held-out evaluation against the exact tracer, then the
-    surrogate-with-fallback pipeline timed against tracing every field."""
+    surrogate-with-fallback pipeline timed against tracing every field (one
+    field per launch, and a chunk of fields per batched launch)."""
     import time
 
     import torch
 
-    from turbulence_tracing_gb300 import fno, surrogate as SG
+    from turbulence_tracing_gb300 import core, fno, surrogate as SG
 
     S = a.sur_size
     W = SG.Workload(S)
@@ -458,6 +459,7 @@ def surrogate_run(a):
     Xte, _, ste, truth, _ = SG.build_dataset(W, SG.draw_fields(a.sur_test, seed=a.seed + 12), keep_truth=True)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
+    target_rms = [float(1.0 / g) for g in W.gain.tolist()]  # rms of the unscaled targets
     net = fno.FNO(S, in_ch=W.in_ch, out_ch=3, layers=4, seed=a.seed)
     trainer = SG.Trainer(net, X, Y, batch=8)
     hist, sps = trainer.fit(a.sur_epochs, lr=1e-3)
@@ -469,51 +471,89 @@ def surrogate_run(a):
     def mean(k):
         return float(np.mean([r[k] for r in held]))
 
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e3 / reps
+
     # inference kernel throughput: forward passes of a batch of 8
     xb = Xte[:8].contiguous()
     ob = net.forward(xb)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(10):
-        net.forward(xb, out=ob)
-    e1.record()
-    torch.cuda.synchronize()
-    us_fwd = e0.elapsed_time(e1) * 1e3 / 80
+    us_fwd = timed(lambda: net.forward(xb, out=ob), 10) / 8
+    ne0 = W.field(SG.draw_fields(1, seed=a.seed + 13)[0])
+    mo = torch.empty((W.n_maps, S, S), dtype=torch.float32, device=W.dev)
+    so = torch.empty((3, S, S), dtype=torch.float32, device=W.dev)
+    us_march = timed(lambda: W.march(ne0, out=mo), 20)
+    f8 = [W.field(p_) for p_ in SG.draw_fields(8, seed=a.seed + 14)]
+    mb = torch.empty((8, W.n_maps, S, S), dtype=torch.float32, device=W.dev)
+    wsb = torch.empty(core.march_batched_workspace_bytes(8, f8[0].shape), dtype=torch.uint8, device=W.dev)
+    us_march_b = timed(lambda: core.march_maps_batched(f8, W.x, W.x, W.x, S, lwl=W.lwl, out=mb, ws=wsb), 10) / 8
+    del f8, mb, wsb
+    us_maps = timed(lambda: W.maps(ne0, out=so), 20)
     C = 32
     fwd_bytes = 4 * (6 * C * S * S * 1 + 16 * C * 32 * S) + (4 * W.in_ch + 2 * C) * S * S + (2 * C + 12) * S * S
+    march_bytes = 4 * S ** 3 * 3 + 20 * S * S  # density read, plane-major q written and read once, 5 maps
     peak, peak_kind = peaks()
     # the pipeline against tracing every held-out field
     params = SG.draw_fields(a.sur_test, seed=a.seed + 12)[half:]
     fields = [W.field(p) for p in params]
+    # detector set-up: each field's drift for 20% straight-line contrast
+    Ds = [float(W.drift(W.maps(f))) for f in fields]
     pipe = SG.Pipeline(W, net, kappa)
-    pipe.run(fields[:2])
-    pipe.run_tracer(fields[:2])
+    bt = SG.BatchedTracer(W)
+    pipe.run(fields[:8], Ds[:8])
+    pipe.run_tracer(fields[:2], Ds[:2])
+    bt.run(fields[:8], Ds[:8])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    I_p, fell = pipe.run(fields)
+    I_p, fell = pipe.run(fields, Ds)
     torch.cuda.synchronize()
     t_pipe = time.perf_counter() - t0
     t0 = time.perf_counter()
-    I_t = pipe.run_tracer(fields)
+    I_t = pipe.run_tracer(fields, Ds)
     torch.cuda.synchronize()
     t_tr = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    I_b = bt.run(fields, Ds)
+    torch.cuda.synchronize()
+    t_bt = time.perf_counter() - t0
     errs = [SG.rel_l2(p_, t_) for p_, t_ in zip(I_p, I_t)]
     acc = [e for e, f in zip(errs, fell) if not f]
+    bt_dev = max(SG.rel_l2(b_, t_) for b_, t_ in zip(I_b, I_t))
     return {"grid": S, "train_fields": a.sur_train, "test_fields": a.sur_test, "epochs": a.sur_epochs,
             "data_s": t_data, "train_samples_per_s": sps, "loss_first_last": [hist[0], hist[-1]],
-            "heldout": {"shadow_err_straight": mean("err_straight"), "shadow_err_net": mean("err_net"),
-                        "theta_err_straight": mean("theta_err_straight"), "theta_err_net": mean("theta_err_net"),
+            "target_rms": target_rms,
+            "heldout": {"shadow_err_straight": mean("err_straight"), "shadow_err_march": mean("err_march"),
+                        "shadow_err_net": mean("err_net"),
+                        "shadow_err_max": {k: max(r[k] for r in held) for k in ("err_straight", "err_march", "err_net")},
+                        "theta_err_straight": mean("theta_err_straight"), "theta_err_march": mean("theta_err_march"),
+                        "theta_err_net": mean("theta_err_net"),
+                        "phase_corr_err_march": mean("phase_corr_err_march"),
                         "phase_corr_err_net": mean("phase_corr_err_net"), "fields": len(held)},
             "fno_forward_us_per_field": us_fwd,
             "fno_forward_roofline": {"bound": "hbm", "achieved": fwd_bytes / (us_fwd * 1e-6) / 1e9, "peak": peak,
                                      "unit": "GB/s", "frac": fwd_bytes / (us_fwd * 1e-6) / 1e9 / peak,
                                      "bytes_per_field": fwd_bytes, "peak_kind": peak_kind},
+            "march_us_per_field": us_march, "march_batched8_us_per_field": us_march_b,
+            "straight_maps_us_per_field": us_maps,
+            "march_roofline": {"bound": "hbm", "achieved": march_bytes / (us_march_b * 1e-6) / 1e9, "peak": peak,
+                               "unit": "GB/s", "frac": march_bytes / (us_march_b * 1e-6) / 1e9 / peak,
+                               "launch": "8 fields per launch",
+                               "bytes_per_field": march_bytes, "peak_kind": peak_kind},
             "pipeline": {"kappa": kappa, "tol": 0.02, "fallback_fraction": float(np.mean(fell)),
-                         "accepted_err_max": max(acc) if acc else None,
+                         "err_max": max(errs), "accepted_err_max": max(acc) if acc else None,
                          "accepted_err_mean": float(np.mean(acc)) if acc else None,
-                         "pipeline_s": t_pipe, "tracer_only_s": t_tr, "speedup_vs_tracer": t_tr / t_pipe},
+                         "pipeline_s": t_pipe, "tracer_per_field_s": t_tr, "tracer_batched_s": t_bt,
+                         "batched_vs_per_field_max_dev": bt_dev,
+                         "speedup_vs_tracer_per_field": t_tr / t_pipe,
+                         "speedup_vs_tracer_batched": t_bt / t_pipe},
             "error_flag": net.error_flag()}
 
 

@@ -279,9 +279,40 @@ int tt_philox(uint64_t seed, uint32_t tag, int64_t count, uint32_t* out, void* s
  *   deflection integrals over that slab,
  * q = min(ne / n_c, ne_max) with n_c and k0 = omega / c as calc_dndr forms them
  * (particle_tracker.py:227-232), gradients by numpy.gradient's rule, all fields
- * trilinear.  x, y, z: host arrays of uniform node coordinates. */
+ * trilinear (the phase by 2-point Gauss per cell).  x, y, z: host arrays of
+ * uniform node coordinates. */
 int tt_straight_line_maps(const void* ne, int ne_dtype, int nx, int ny, int nz, const double* x, const double* y,
                           const double* z, double lwl, double ne_max, int P, int nslab, float* out, void* stream);
+
+/* Marched pixel-centre rays, the surrogate's coarse solution: the same P x P
+ * pixel-centre rays as tt_straight_line_maps, entering along +z at z0 and
+ * stepped from node plane to node plane (one step per cell along z, second
+ * order) through the ray equation with z as the parameter,
+ *   dt/dz = -1/2 (1 + |t|^2) / (1 + q0 - q) (grad_perp q - t dq/dz),
+ * t the slopes (dx/dz, dy/dz), q0 = q at the entry point, fields as the tracer
+ * interpolates them (numpy.gradient derivatives, bilinear on the node planes,
+ * zero outside).  out FP32 [5][P][P]: the marched exit angles arctan(t_x),
+ * arctan(t_y) (rad, as ray_at_exit, particle_tracker.py:333-380) and phase
+ * k0 integral (sqrt(1 - q) - 1) ds (rad), then the straight-line deflection of
+ * the same rays (tt_straight_line_maps' first two outputs), all from one pass
+ * over the density.  workspace: device scratch of
+ * tt_march_maps_workspace_bytes(nx, ny, nz) bytes, 16-byte aligned (q stored
+ * plane by plane with a ghost border, and its column sums); nx <= 65535. */
+size_t tt_march_maps_workspace_bytes(int nx, int ny, int nz);
+int tt_march_maps(const void* ne, int ne_dtype, int nx, int ny, int nz, const double* x, const double* y,
+                  const double* z, double lwl, double ne_max, int P, float* out, void* workspace,
+                  size_t workspace_bytes, void* stream);
+
+/* tt_march_maps over nfields (1..TT_MAX_MARCH_FIELDS) fields of one shape in
+ * one pass: ne is a host array of nfields device pointers, out FP32
+ * [nfields][5][P][P], workspace of tt_march_maps_batched_workspace_bytes
+ * bytes.  Fields march side by side, which fills the GPU where one field's
+ * P x P rays do not. */
+#define TT_MAX_MARCH_FIELDS 32
+size_t tt_march_maps_batched_workspace_bytes(int nfields, int nx, int ny, int nz);
+int tt_march_maps_batched(const void* const* ne, int nfields, int ne_dtype, int nx, int ny, int nz, const double* x,
+                          const double* y, const double* z, double lwl, double ne_max, int P, float* out,
+                          void* workspace, size_t workspace_bytes, void* stream);
 
 /* Geometric-optics shadowgram of a deflection map theta FP32 [2][P][P] (angles
  * of rays leaving the centres of a P x P pixel grid of pitch `pitch` m):

@@ -31,6 +31,151 @@ def _maps_restated(ne, x, lwl, S):
     return -0.5 * (bil(gx) * w).sum(-1), -0.5 * (bil(gy) * w).sum(-1)
 
 
+def _march_restated(ne, x, lwl, P):
+    """The plane march in float64: q = min(ne/n_c, 1), numpy.gradient
+    derivatives, bilinear on the node planes (zero outside the grid), and
+    kick-drift-kick in z from plane to plane on the ray equation with the
+    second kick's slope-dependent term iterated once; trapezoid phase in ds.
+    Then the straight ray from the same pixel centre: trapezoid deflection
+    integrals on the planes."""
+    omega, nc = R.critical_density(lwl)
+    q = np.minimum(ne / nc, 1.0)
+    n, h = len(x), x[1] - x[0]
+    fields = (q, np.gradient(q, axis=0) / h, np.gradient(q, axis=1) / h, np.gradient(q, axis=2) / h)
+    c = (np.arange(P) + 0.5) / P * (n - 1)
+    u, v = np.repeat(c, P), np.tile(c, P)
+
+    def sample(u, v, k):
+        ins = (u >= 0) & (u <= n - 1) & (v >= 0) & (v <= n - 1)
+        i = np.clip(np.floor(np.where(ins, u, 0)).astype(int), 0, n - 2)
+        j = np.clip(np.floor(np.where(ins, v, 0)).astype(int), 0, n - 2)
+        fx, fy = np.where(ins, u, 0) - i, np.where(ins, v, 0) - j
+        out = []
+        for F in fields:
+            Fk = F[:, :, k]
+            val = ((1 - fx) * (1 - fy) * Fk[i, j] + fx * (1 - fy) * Fk[i + 1, j] + (1 - fx) * fy * Fk[i, j + 1]
+                   + fx * fy * Fk[i + 1, j + 1])
+            out.append(np.where(ins, val, 0.0))
+        return out
+
+    def accel(f, tx, ty, q0):
+        cf = -0.5 * (1 + tx * tx + ty * ty) / (1 + q0 - f[0])
+        return cf * (f[1] - tx * f[3]), cf * (f[2] - ty * f[3])
+
+    def dphase(f, tx, ty):
+        return (np.sqrt(np.maximum(1 - f[0], 0)) - 1) * np.sqrt(1 + tx * tx + ty * ty)
+
+    u0, v0 = u.copy(), v.copy()
+    f = sample(u, v, 0)
+    q0 = f[0]
+    tx, ty = np.zeros_like(u), np.zeros_like(u)
+    ax, ay = accel(f, tx, ty, q0)
+    e, phi = dphase(f, tx, ty), np.zeros_like(u)
+    for k in range(1, n):
+        d = h
+        tx, ty = tx + d / 2 * ax, ty + d / 2 * ay
+        u, v = u + tx, v + ty
+        f = sample(u, v, k)
+        bx, by = accel(f, tx, ty, q0)
+        ax, ay = accel(f, tx + d / 2 * bx, ty + d / 2 * by, q0)
+        tx, ty = tx + d / 2 * ax, ty + d / 2 * ay
+        e2 = dphase(f, tx, ty)
+        phi += d / 2 * (e + e2)
+        e = e2
+    k0 = omega / R.C_LIGHT
+    # the straight ray
+    sxs, sys_ = np.zeros_like(u), np.zeros_like(u)
+    for k in range(n):
+        f = sample(u0, v0, k)
+        w = 0.5 if k in (0, n - 1) else 1.0
+        sxs += w * f[1]
+        sys_ += w * f[2]
+    return np.stack([np.arctan(tx), np.arctan(ty), k0 * phi, -0.5 * h * sxs, -0.5 * h * sys_]).reshape(5, P, P)
+
+
+@pytest.mark.parametrize("n,P", [(40, 32), (40, 40), (44, 60), (48, 47), (48, 24)])
+def test_march_maps_match_restatement(cuda, n, P):
+    """The staged tile kernel (pixel grid at least as fine as the node grid:
+    P >= n - 1; the tiles at the grid's faces read the ghost border) and, for
+    P = 32 on 40 nodes and P = 24 on 48, the unstaged one."""
+    from turbulence_tracing_gb300 import core
+
+    ne, x = R.workload_density(n, 1e-3, -3.0, 0.25, 2e25, 4)
+    m = core.march_maps(ne, x, x, x, P, lwl=1064e-9).cpu().numpy()
+    ref = _march_restated(ne, x, 1064e-9, P)
+    scale = np.abs(ref[0:2]).max()
+    for c in (0, 1, 3, 4):
+        assert np.abs(m[c] - ref[c]).max() <= 1e-4 * scale, c
+    assert np.abs(m[2] - ref[2]).max() <= 1e-4 * np.abs(ref[2]).max()
+    # the straight-ray maps are tt_straight_line_maps' answer
+    st = core.straight_line_maps(ne, x, x, x, P, lwl=1064e-9).cpu().numpy()
+    assert np.abs(m[3:5] - st[0:2]).max() <= 1e-5 * scale
+    # the rays bend: the march is not the straight-line answer
+    assert np.abs(m[0] - st[0]).max() > 1e-2 * scale
+
+
+def test_march_far_drift_reads_outside_the_staged_window(cuda):
+    """Rays that drift further than the staged halo (8 cells) take their
+    samples from global memory; the answer is the same."""
+    from turbulence_tracing_gb300 import core
+
+    n = 40
+    ne, x = R.workload_density(n, 1e-3, -5.0 / 3.0, 0.3, 2e26, 6)
+    m = core.march_maps(ne, x, x, x, n, lwl=1064e-9).cpu().numpy()
+    ref = _march_restated(ne, x, 1064e-9, n)
+    # exit slopes times the box length in cells bound the drift from below
+    assert np.abs(np.tan(ref[0:2])).max() * (n - 1) / 2 > 8
+    scale = np.abs(ref[0:2]).max()
+    for c in (0, 1, 3, 4):
+        assert np.abs(m[c] - ref[c]).max() <= 1e-3 * scale, c
+    assert np.abs(m[2] - ref[2]).max() <= 1e-3 * np.abs(ref[2]).max()
+
+
+def test_march_plain_kernel_matches_restatement(cuda):
+    """A pixel grid coarser than the node grid takes the unstaged kernel; a
+    grid width that is not a multiple of 4 pads its rows."""
+    from turbulence_tracing_gb300 import core
+
+    ne, x = R.workload_density(42, 1e-3, -3.0, 0.25, 2e25, 5)
+    m = core.march_maps(ne, x, x, x, 30, lwl=1064e-9).cpu().numpy()
+    ref = _march_restated(ne, x, 1064e-9, 30)
+    scale = np.abs(ref[0:2]).max()
+    for c in (0, 1, 3, 4):
+        assert np.abs(m[c] - ref[c]).max() <= 1e-4 * scale, c
+    assert np.abs(m[2] - ref[2]).max() <= 1e-4 * np.abs(ref[2]).max()
+
+
+def test_march_batched_equals_single_fields(cuda):
+    from turbulence_tracing_gb300 import core
+
+    n = 44
+    fields = [torch.as_tensor(R.workload_density(n, 1e-3, a, 0.25, 2e25, sd)[0], dtype=torch.float32, device="cuda")
+              for a, sd in ((-3.0, 1), (-5.0 / 3.0, 2), (-11.0 / 3.0, 3))]
+    x = np.linspace(-0.5e-3, 0.5e-3, n)
+    for P in (n, 30):  # staged and unstaged kernels
+        b = core.march_maps_batched(fields, x, x, x, P, lwl=1064e-9)
+        for i, f in enumerate(fields):
+            assert torch.equal(b[i], core.march_maps(f, x, x, x, P, lwl=1064e-9)), (P, i)
+
+
+def test_march_is_close_to_exact_trace(cuda):
+    """One field sample per cell and second order in z: on a field whose rays
+    drift by cells the marched shadowgram is within 2% of the exact trace's,
+    where the straight-line one is far off."""
+    from turbulence_tracing_gb300 import surrogate as SG
+
+    W = SG.Workload(128)
+    ne = W.field(dict(alpha=-11 / 3, delta=0.3, ne0=8e24, seed=7))
+    m, mm = W.maps(ne), W.march(ne)
+    theta, phase, _ = W.trace(ne)
+    D = W.drift(m)
+    I_t = W.shadow(theta, D)
+    e_s, e_m = SG.rel_l2(W.shadow(m[0:2], D), I_t), SG.rel_l2(W.shadow(mm[0:2], D), I_t)
+    assert e_m <= 0.02 and e_m <= 0.25 * e_s, (e_m, e_s)
+    corr = float((phase - m[2].double()).norm())
+    assert float((phase - mm[2].double()).norm()) <= 0.3 * corr
+
+
 def test_straight_line_maps_match_restatement(cuda):
     from turbulence_tracing_gb300 import core
 
@@ -62,28 +207,34 @@ def test_straight_line_map_is_first_order_trace(cuda):
     assert 1.5 < errs[0] / errs[1] < 2.7, errs
 
 
-def test_trained_surrogate_beats_straight_line_and_fallback_bounds_error(cuda):
+def test_trained_surrogate_gains_and_fallback_bounds_error(cuda):
     from turbulence_tracing_gb300 import fno, surrogate as SG
 
     W = SG.Workload(128)
     Xtr, Ytr, _, _, _ = SG.build_dataset(W, SG.draw_fields(384, seed=1))
     Xte, _, ste, truth, _ = SG.build_dataset(W, SG.draw_fields(48, seed=2), keep_truth=True)
+    # the training targets are scaled to unit rms per channel
+    assert torch.allclose(torch.sqrt((Ytr.double() ** 2).mean(dim=(0, 2, 3))), torch.ones(3, dtype=torch.float64,
+                                                                                           device=Ytr.device), rtol=1e-3)
     net = fno.FNO(128, in_ch=W.in_ch, out_ch=3, layers=4, seed=0)
     hist, _ = SG.Trainer(net, Xtr, Ytr, batch=8).fit(12, lr=1e-3)
-    assert hist[-1] < 0.7 * hist[0], hist
+    assert hist[-1] < 0.8 * hist[0], hist
     res = SG.evaluate(W, net, Xte, ste, truth)
     assert net.error_flag() == 0
     e_s = np.array([r["err_straight"] for r in res])
+    e_m = np.array([r["err_march"] for r in res])
     e_n = np.array([r["err_net"] for r in res])
-    ph = np.array([r["phase_corr_err_net"] for r in res])
-    strong = e_s > 0.02
-    # the network's shadowgrams are closer to the exact trace than the straight-line ones
-    assert e_n[strong].mean() < 0.95 * e_s[strong].mean(), (e_n[strong].mean(), e_s[strong].mean())
-    # and it recovers part of the phase correction the straight-line method misses entirely
-    assert np.median(ph) < 1.0, np.median(ph)
+    ph_n = np.array([r["phase_corr_err_net"] for r in res])
+    # against the method without the network -- the straight-line maps it is given --
+    # the shadowgrams are an order of magnitude closer to the exact trace
+    assert e_n.mean() < 0.1 * e_s.mean(), (e_n.mean(), e_s.mean())
+    assert np.median(ph_n) < 0.2, np.median(ph_n)
+    # and the network does not spoil the march it corrects
+    assert e_n.mean() <= 1.5 * e_m.mean(), (e_n.mean(), e_m.mean())
     # fallback: fields whose estimate exceeds the tolerance are traced; the accepted
-    # ones stay within tolerance for the calibrated quantile
+    # ones stay within tolerance
     kappa = SG.calibrate(res[:24])
     est = np.array([kappa * r["moved"] for r in res[24:]])
     acc = est <= 0.02
-    assert np.all(e_n[24:][acc] <= 0.03), e_n[24:][acc]
+    assert acc.mean() >= 0.5
+    assert np.all(e_n[24:][acc] <= 0.02), e_n[24:][acc]

@@ -34,6 +34,7 @@ OPTIC_KNIFE_EDGE = 6
 OPTIC_M_TO_MM = 7
 MAX_OPTICS = 64
 MAX_INSTANCES = 128
+MAX_MARCH_FIELDS = 32
 
 
 class TTError(RuntimeError):
@@ -121,6 +122,13 @@ SIGNATURES = {
     "tt_philox": (c_int, [ctypes.c_uint64, ctypes.c_uint32, c_i64, c_void_p, c_void_p]),
     "tt_straight_line_maps": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_double_p, c_double_p, c_double_p,
                                       ctypes.c_double, ctypes.c_double, c_int, c_int, c_void_p, c_void_p]),
+    "tt_march_maps_workspace_bytes": (c_size, [c_int, c_int, c_int]),
+    "tt_march_maps_batched_workspace_bytes": (c_size, [c_int, c_int, c_int, c_int]),
+    "tt_march_maps_batched": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_int, c_int, c_int, c_double_p,
+                                      c_double_p, c_double_p, ctypes.c_double, ctypes.c_double, c_int, c_void_p,
+                                      c_void_p, c_size, c_void_p]),
+    "tt_march_maps": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_double_p, c_double_p, c_double_p,
+                              ctypes.c_double, ctypes.c_double, c_int, c_void_p, c_void_p, c_size, c_void_p]),
     "tt_shadowgram": (c_int, [c_void_p, c_int, ctypes.c_double, ctypes.c_double, c_void_p, c_void_p, c_void_p]),
     "tt_fno_param_count": (c_size, [ctypes.POINTER(TTFnoDims)]),
     "tt_fno_workspace_bytes": (c_size, [ctypes.POINTER(TTFnoDims), c_int]),

@@ -340,6 +340,66 @@ def straight_line_maps(ne, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, nslab=
     return out
 
 
+def march_workspace_bytes(shape):
+    nx, ny, nz = (int(v) for v in shape)
+    return int(_lib.lib().tt_march_maps_workspace_bytes(nx, ny, nz))
+
+
+def march_batched_workspace_bytes(nfields, shape):
+    nx, ny, nz = (int(v) for v in shape)
+    return int(_lib.lib().tt_march_maps_batched_workspace_bytes(int(nfields), nx, ny, nz))
+
+
+def march_maps_batched(fields, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, ws=None):
+    """march_maps over a list of same-shape density tensors in one pass
+    (tt_march_maps_batched): (len(fields), 5, P, P) float32."""
+    dev = require_cuda()
+    nf = len(fields)
+    if not (1 <= nf <= _lib.MAX_MARCH_FIELDS):
+        raise ValueError("1..%d fields per call" % _lib.MAX_MARCH_FIELDS)
+    ts = [_dens_dev(f, dev) for f in fields]
+    shape, dt = tuple(ts[0].shape), ts[0].dtype
+    if any(tuple(t.shape) != shape or t.dtype != dt for t in ts):
+        raise ValueError("fields must share shape and dtype")
+    nx, ny, nz = shape
+    xa, ya, za = (np.ascontiguousarray(np.asarray(c, dtype=np.float64)) for c in (x, y, z))
+    if out is None:
+        out = torch.empty((nf, 5, P, P), dtype=torch.float32, device=dev)
+    L = _lib.lib()
+    need = int(L.tt_march_maps_batched_workspace_bytes(nf, nx, ny, nz))
+    if ws is None or ws.numel() < need:
+        ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    ptrs = (ctypes.c_void_p * nf)(*[t.data_ptr() for t in ts])
+    dp = ctypes.POINTER(ctypes.c_double)
+    check(L.tt_march_maps_batched(ptrs, nf, _dtype_code(ts[0]), nx, ny, nz, xa.ctypes.data_as(dp),
+                                  ya.ctypes.data_as(dp), za.ctypes.data_as(dp), float(lwl), float(ne_max), int(P),
+                                  _ptr(out), _ptr(ws), need, _stream()), "tt_march_maps_batched")
+    return out
+
+
+def march_maps(ne, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, ws=None):
+    """(5, P, P) float32 from one pass over the density (tt_march_maps): exit
+    angles (x, y) and phase of the pixel-centre rays marched one node plane per
+    step through the ray equation -- the coarse solution the surrogate
+    corrects -- then the straight-line deflection angles of the same rays (as
+    straight_line_maps).  ws: optional uint8 device workspace of at least
+    march_workspace_bytes(ne.shape) bytes, reused across calls."""
+    dev = require_cuda()
+    ne_t = _dens_dev(ne, dev)
+    nx, ny, nz = ne_t.shape
+    xa, ya, za = (np.ascontiguousarray(np.asarray(c, dtype=np.float64)) for c in (x, y, z))
+    if out is None:
+        out = torch.empty((5, P, P), dtype=torch.float32, device=dev)
+    need = march_workspace_bytes((nx, ny, nz))
+    if ws is None or ws.numel() < need:
+        ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    dp = ctypes.POINTER(ctypes.c_double)
+    check(_lib.lib().tt_march_maps(_ptr(ne_t), _dtype_code(ne_t), nx, ny, nz, xa.ctypes.data_as(dp),
+                                   ya.ctypes.data_as(dp), za.ctypes.data_as(dp), float(lwl), float(ne_max), int(P),
+                                   _ptr(out), _ptr(ws), need, _stream()), "tt_march_maps")
+    return out
+
+
 def shadowgram(theta, pitch, D, intensity=None, div=None, want_intensity=True, want_div=False):
     """Geometric-optics shadowgram of a (2, P, P) float32 deflection map (tt_shadowgram).
     Returns (intensity, div); either is None when not asked for."""

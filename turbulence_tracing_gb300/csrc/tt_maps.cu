@@ -13,17 +13,39 @@
 // rule on the node grid (central inside, one-sided at the faces), both
 // interpolated trilinearly -- the same fields the tracer integrates.  The
 // gradient integrals are exact for the trilinear interpolant (trapezoid on
-// nodes); the phase uses 4-point Gauss-Legendre in every z cell.
+// nodes); the phase uses 2-point Gauss-Legendre in every z cell.
 #include "tt_common.cuh"
 
 namespace {
 
 constexpr int kMaxSlab = 8;
 
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float sqrt_approx(float x)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// n - 1 = sqrt(1 - q) - 1 in the form without cancellation for small q
+__device__ __forceinline__ float index_minus_one(float q)
+{
+    const float r = 1.f - q;
+    return -q * rcp_approx(1.f + sqrt_approx(r > 0.f ? r : 0.f));
+}
+
+
 // One warp per pixel: lane l handles nodes k = l, l + 32, ... along z, so
 // the column reads (z is the fastest axis of the density) are coalesced; the
 // per-lane sums are combined with shuffles.
-template <typename T>
+template <typename T, bool SLAB>
 __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, double hx, double hy, double hz,
                             float inv_nc, float ne_max, double k0, int P, int nslab, float* __restrict__ out)
 {
@@ -39,8 +61,6 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
     iy = iy < 0 ? 0 : (iy > ny - 2 ? ny - 2 : iy);
     const float fx = (float)(xs / hx - ix), fy = (float)(ys / hy - iy);
     const float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w01 = (1.f - fx) * fy, w11 = fx * fy;
-    const float gw[4] = {0.0694318442029737f, 0.3300094782075719f, 0.6699905217924281f, 0.9305681557970263f};
-    const float gwt[4] = {0.1739274225687269f, 0.3260725774312731f, 0.3260725774312731f, 0.1739274225687269f};
     // columns: x neighbours ix-1..ix+2 at rows iy, iy+1; y neighbours iy-1..iy+2 at columns ix, ix+1
     const int xm = ix > 0 ? ix - 1 : ix, xp = ix + 2 < nx ? ix + 2 : ix + 1;
     const int ym = iy > 0 ? iy - 1 : iy, yp = iy + 2 < ny ? iy + 2 : iy + 1;
@@ -73,7 +93,7 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
         sy = fmaf(wz, gyk, sy);
         // node k's trapezoid weight is half from cell k-1 and half from cell k,
         // each credited to that cell's slab
-        if (nslab > 0) {
+        if (SLAB) {
 #pragma unroll
             for (int q = 0; q < kMaxSlab; ++q) {
                 const float wl = (k > 0 && (int)((long long)(k - 1) * nslab / (nz - 1)) == q) ? 0.5f : 0.f;
@@ -82,27 +102,24 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
                 sly[q] = fmaf(wl + wr, gyk, sly[q]);
             }
         }
-        if (k + 1 < nz) {  // the cell [k, k+1]: 4-point Gauss-Legendre on the linear q(z)
+        if (k + 1 < nz) {  // the cell [k, k+1]: 2-point Gauss-Legendre on the linear q(z)
             const float qk = w00 * q00 + w10 * q10 + w01 * q01 + w11 * q11;
             const float qn = w00 * q(c00, k + 1) + w10 * q(c10, k + 1) + w01 * q(c01, k + 1) + w11 * q(c11, k + 1);
-            float cell = 0.f;
-#pragma unroll
-            for (int g = 0; g < 4; ++g) {
-                const float r = 1.f - (qk + gw[g] * (qn - qk));
-                cell += gwt[g] * (sqrtf(r > 0.f ? r : 0.f) - 1.f);
-            }
-            sp += cell;
+            const float g = 0.2113248654051871f;  // 1/2 - 1/(2 sqrt 3)
+            sp += 0.5f * (index_minus_one(fmaf(g, qn - qk, qk)) + index_minus_one(fmaf(g, qk - qn, qn)));
         }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         sx += __shfl_xor_sync(0xffffffffu, sx, off);
         sy += __shfl_xor_sync(0xffffffffu, sy, off);
+        if (SLAB) {
 #pragma unroll
-        for (int q = 0; q < kMaxSlab; ++q) {
-            if (q < nslab) {
-                slx[q] += __shfl_xor_sync(0xffffffffu, slx[q], off);
-                sly[q] += __shfl_xor_sync(0xffffffffu, sly[q], off);
+            for (int q = 0; q < kMaxSlab; ++q) {
+                if (q < nslab) {
+                    slx[q] += __shfl_xor_sync(0xffffffffu, slx[q], off);
+                    sly[q] += __shfl_xor_sync(0xffffffffu, sly[q], off);
+                }
             }
         }
         sp += __shfl_xor_sync(0xffffffffu, sp, off);
@@ -111,11 +128,13 @@ __global__ void maps_kernel(const T* __restrict__ ne, int nx, int ny, int nz, do
         out[warp] = (float)(-0.5 * (double)sx * hz / hx);
         out[n + warp] = (float)(-0.5 * (double)sy * hz / hy);
         out[2 * n + warp] = (float)(k0 * (double)sp * hz);
+        if (SLAB) {
 #pragma unroll
-        for (int q = 0; q < kMaxSlab; ++q) {
-            if (q < nslab) {
-                out[(3 + 2 * q) * n + warp] = (float)(-0.5 * (double)slx[q] * hz / hx);
-                out[(4 + 2 * q) * n + warp] = (float)(-0.5 * (double)sly[q] * hz / hy);
+            for (int q = 0; q < kMaxSlab; ++q) {
+                if (q < nslab) {
+                    out[(3 + 2 * q) * n + warp] = (float)(-0.5 * (double)slx[q] * hz / hx);
+                    out[(4 + 2 * q) * n + warp] = (float)(-0.5 * (double)sly[q] * hz / hy);
+                }
             }
         }
     }
@@ -141,13 +160,511 @@ extern "C" int tt_straight_line_maps(const void* ne, int ne_dtype, int nx, int n
     const long long threads = (long long)n * 32;
     const int grid = (int)((threads + 255) / 256);
     cudaStream_t s = tt::as_stream(stream);
-    if (ne_dtype == TT_F32)
-        maps_kernel<float><<<grid, 256, 0, s>>>((const float*)ne, nx, ny, nz, hx, hy, hz, (float)(1.0 / nc),
-                                                (float)ne_max, k0, P, nslab, out);
-    else
-        maps_kernel<double><<<grid, 256, 0, s>>>((const double*)ne, nx, ny, nz, hx, hy, hz, (float)(1.0 / nc),
-                                                 (float)ne_max, k0, P, nslab, out);
+    const float inv_nc = (float)(1.0 / nc), qmax = (float)ne_max;
+    if (ne_dtype == TT_F32) {
+        if (nslab > 0)
+            maps_kernel<float, true><<<grid, 256, 0, s>>>((const float*)ne, nx, ny, nz, hx, hy, hz, inv_nc, qmax, k0,
+                                                          P, nslab, out);
+        else
+            maps_kernel<float, false><<<grid, 256, 0, s>>>((const float*)ne, nx, ny, nz, hx, hy, hz, inv_nc, qmax, k0,
+                                                           P, nslab, out);
+    } else {
+        if (nslab > 0)
+            maps_kernel<double, true><<<grid, 256, 0, s>>>((const double*)ne, nx, ny, nz, hx, hy, hz, inv_nc, qmax,
+                                                           k0, P, nslab, out);
+        else
+            maps_kernel<double, false><<<grid, 256, 0, s>>>((const double*)ne, nx, ny, nz, hx, hy, hz, inv_nc, qmax,
+                                                            k0, P, nslab, out);
+    }
     return tt::launch_status("straight_line_maps");
+}
+
+// Marched pixel-centre rays: the ray equation with z as the parameter and
+// t = (dx/dz, dy/dz) the ray's slopes,
+//   dt/dz   = -1/2 (1 + |t|^2) / (1 + q0 - q) * (grad_perp q - t dq/dz)
+//   dphi/dz = k0 (sqrt(1 - q) - 1) sqrt(1 + |t|^2)
+// (from dx/dt = v, dv/dt = -c^2/2 grad q and |v|^2 = c^2 (1 + q0 - q), q0 the
+// value at the entry point), stepped from node plane to node plane (step hz)
+// by kick-drift-kick with the second kick's slope-dependent term iterated once
+// (second order), the phase summed in FP32 with Neumaier compensation.  Every
+// plane is visited: skipping planes aliases the grid-scale gradient (the
+// trapezoid rule on a field with power at the node spacing).  On a plane the
+// fields are bilinear in x, y of the node values -- q and its numpy.gradient
+// derivatives, zero outside the grid, i.e. the tracer's trilinear fields
+// restricted to the node planes.
+//
+// Layout.  q = min(ne / n_c, ne_max) is first written plane-major into the
+// workspace, [z][x + 1][y + 4] with a one-node ghost border around each plane
+// holding the linear extrapolation 2 q(edge) - q(edge -+ 1): the central
+// difference across the border then equals numpy.gradient's one-sided
+// difference at the face, so every in-grid sample uses one branch-free
+// stencil.  Rows are padded to a multiple of 4 floats so that y = 0 and every
+// staged chunk start on 16 bytes.  The same pass sums q along z per column with
+// trapezoid weights; the straight (unbent) ray's deflection is linear in q, so
+// a small 2-D kernel turns those sums into the straight-line maps (the same
+// definition as tt_straight_line_maps: exact for the trilinear field).
+//
+// The march: one thread per ray; tiles of kMarchRows x 32 rays (a warp = one
+// row of 32 rays, so the staged reads are free of bank conflicts) stage the
+// node rows and columns their rays can reach (the tile plus kMarchHalo cells),
+// plane by plane, into a ring of kMarchRing planes in shared memory with
+// cp.async, kMarchRing - 2 planes ahead of the march.  A ray whose stencil
+// leaves the staged window (a drift of more than about kMarchHalo - 2 cells)
+// reads that sample from global memory; the results are the same either way.
+// Pixel grids coarser than the node grid take the unstaged kernel.
+namespace {
+
+constexpr int kPadY = 4;  // padded column of y = 0
+
+__host__ __device__ inline int padded_ny(int ny) { return (ny + kPadY + 1 + 3) & ~3; }
+__host__ __device__ inline size_t padded_plane(int nx, int ny) { return (size_t)(nx + 2) * padded_ny(ny); }
+
+struct MarchFields {
+    const void* ne[TT_MAX_MARCH_FIELDS];
+};
+
+// Per-field workspace (floats): the padded planes, then the column sums.
+inline size_t field_ws_floats(int nx, int ny, int nz)
+{
+    const size_t f = (size_t)nz * padded_plane(nx, ny) + (size_t)nx * ny;
+    return (f + 63) & ~(size_t)63;  // 256-byte aligned per field
+}
+
+// q -> padded plane-major, and the trapezoid column sums Sum_k w_k q(x, y, k).
+// Block: one x, 32 columns y of field blockIdx.z; loops over z in tiles of 32
+// through shared memory (read along z, write along y).
+template <typename T>
+__global__ void __launch_bounds__(256) plane_q_kernel(const __grid_constant__ MarchFields fields, int nx, int ny,
+                                                     int nz, float inv_nc, float ne_max, float* __restrict__ ws,
+                                                     size_t ws_field)
+{
+    __shared__ float tile[32][33];
+    const T* __restrict__ ne = static_cast<const T*>(fields.ne[blockIdx.z]);
+    float* __restrict__ qt = ws + blockIdx.z * ws_field;
+    float* __restrict__ colsum = qt + (size_t)nz * padded_plane(nx, ny);
+    const int a = blockIdx.y;
+    const int y0 = blockIdx.x * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+    const int nyp = padded_ny(ny);
+    const size_t plane = padded_plane(nx, ny);
+    float acc = 0.f;  // column y0 + tx, summed by warp 0
+    for (int z0 = 0; z0 < nz; z0 += 32) {
+        for (int r = ty; r < 32; r += 8) {
+            const int y = y0 + r, z = z0 + tx;
+            float v = 0.f;
+            if (y < ny && z < nz) {
+                v = (float)ne[((size_t)a * ny + y) * nz + z] * inv_nc;
+                v = v < ne_max ? v : ne_max;
+            }
+            tile[r][tx] = v;
+        }
+        __syncthreads();
+        for (int r = ty; r < 32; r += 8) {
+            const int z = z0 + r, y = y0 + tx;
+            if (y < ny && z < nz) qt[(size_t)z * plane + (size_t)(a + 1) * nyp + y + kPadY] = tile[tx][r];
+        }
+        if (ty == 0) {
+            const int zend = min(32, nz - z0);
+            for (int r = 0; r < zend; ++r) {
+                const int z = z0 + r;
+                acc = fmaf((z == 0 || z == nz - 1) ? 0.5f : 1.f, tile[tx][r], acc);
+            }
+        }
+        __syncthreads();
+    }
+    if (ty == 0 && y0 + tx < ny) colsum[(size_t)a * ny + y0 + tx] = acc;
+}
+
+// Ghost border of every plane: rows x = -1, nx (over y in [0, ny)) and columns
+// y = -1, ny (over x in [0, nx)) as 2 q(edge) - q(next).  The four corner
+// ghosts are never read by the stencil and are left as they are.
+__global__ void plane_ghost_kernel(int nfields, int nx, int ny, int nz, float* __restrict__ ws, size_t ws_field)
+{
+    const int nyp = padded_ny(ny);
+    const size_t plane = padded_plane(nx, ny);
+    const long long per = 2LL * ny + 2LL * nx;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= per * nz * nfields) return;
+    const int f = (int)(t / (per * nz));
+    const long long tf = t - (long long)f * per * nz;
+    const int z = (int)(tf / per);
+    int e = (int)(tf - (long long)z * per);
+    float* pl = ws + f * ws_field + (size_t)z * plane;
+    auto at = [&](int x, int y) -> float& { return pl[(size_t)(x + 1) * nyp + y + kPadY]; };
+    if (e < ny) {
+        at(-1, e) = 2.f * at(0, e) - at(1, e);
+    } else if ((e -= ny) < ny) {
+        at(nx, e) = 2.f * at(nx - 1, e) - at(nx - 2, e);
+    } else if ((e -= ny) < nx) {
+        at(e, -1) = 2.f * at(e, 0) - at(e, 1);
+    } else {
+        e -= nx;
+        at(e, ny) = 2.f * at(e, ny - 1) - at(e, ny - 2);
+    }
+}
+
+// Straight-line deflection at the pixel centres from the column sums:
+// -1/2 hz d/dx of the trapezoid sum (numpy.gradient rule), bilinear.
+__global__ void straight_from_colsum_kernel(const float* __restrict__ ws, size_t ws_field, int nx, int ny, int nz,
+                                            float cx, float cy, int P, float* __restrict__ out)
+{
+    const int n = P * P;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int f = blockIdx.y;
+    const float* __restrict__ colsum = ws + f * ws_field + (size_t)nz * padded_plane(nx, ny);
+    float* __restrict__ ox = out + ((size_t)f * 5 + 3) * n;
+    float* __restrict__ oy = ox + n;
+    const int pi = p / P, pj = p % P;
+    const double us = ((pi + 0.5) / P) * (nx - 1), vs = ((pj + 0.5) / P) * (ny - 1);
+    const int i = min((int)us, nx - 2), j = min((int)vs, ny - 2);
+    const float fx = (float)(us - i), fy = (float)(vs - j);
+    auto C = [&](int a, int b) { return colsum[(size_t)a * ny + b]; };
+    auto gx = [&](int a, int b) {
+        if (a == 0) return C(1, b) - C(0, b);
+        if (a == nx - 1) return C(nx - 1, b) - C(nx - 2, b);
+        return 0.5f * (C(a + 1, b) - C(a - 1, b));
+    };
+    auto gy = [&](int a, int b) {
+        if (b == 0) return C(a, 1) - C(a, 0);
+        if (b == ny - 1) return C(a, ny - 1) - C(a, ny - 2);
+        return 0.5f * (C(a, b + 1) - C(a, b - 1));
+    };
+    const float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w01 = (1.f - fx) * fy, w11 = fx * fy;
+    ox[p] = cx * (w00 * gx(i, j) + w10 * gx(i + 1, j) + w01 * gx(i, j + 1) + w11 * gx(i + 1, j + 1));
+    oy[p] = cy * (w00 * gy(i, j) + w10 * gy(i + 1, j) + w01 * gy(i, j + 1) + w11 * gy(i + 1, j + 1));
+}
+
+struct PlaneSample {
+    float q, gx, gy, gz;  // q and its derivatives per index unit
+};
+
+// The cell of (u, v) (index units) on a node plane; false outside the grid,
+// where every field is zero.
+__device__ __forceinline__ bool locate(float u, float v, int nx, int ny, int& i, int& j, float& fx, float& fy)
+{
+    if (!(u >= 0.f && u <= (float)(nx - 1) && v >= 0.f && v <= (float)(ny - 1))) return false;
+    i = min((int)u, nx - 2);
+    j = min((int)v, ny - 2);
+    fx = u - (float)i;
+    fy = v - (float)j;
+    return true;
+}
+
+// q and its derivatives at (i + fx, j + fy): c points at node (i, j) of the
+// plane, m and p at that node of the planes used for d/dz (dz = 1/2 inside,
+// 1 at the first and last plane, where they are the plane itself and its
+// neighbour); ry is the row stride.  Central differences throughout: the ghost
+// border supplies the one-sided rule at the faces.
+template <typename Stride>
+__device__ __forceinline__ PlaneSample sample_node(const float* c, const float* m, const float* p, Stride ry, float dz,
+                                                   float fx, float fy)
+{
+    const float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w01 = (1.f - fx) * fy, w11 = fx * fy;
+    const float q00 = c[0], q10 = c[ry], q01 = c[1], q11 = c[ry + 1];
+    const float gx00 = q10 - c[-ry], gx10 = c[2 * ry] - q00;
+    const float gx01 = q11 - c[1 - ry], gx11 = c[2 * ry + 1] - q01;
+    const float gy00 = q01 - c[-1], gy01 = c[2] - q00;
+    const float gy10 = q11 - c[ry - 1], gy11 = c[ry + 2] - q10;
+    const float gz = w00 * (p[0] - m[0]) + w10 * (p[ry] - m[ry]) + w01 * (p[1] - m[1]) + w11 * (p[ry + 1] - m[ry + 1]);
+    PlaneSample s;
+    s.q = w00 * q00 + w10 * q10 + w01 * q01 + w11 * q11;
+    s.gx = 0.5f * (w00 * gx00 + w10 * gx10 + w01 * gx01 + w11 * gx11);
+    s.gy = 0.5f * (w00 * gy00 + w10 * gy10 + w01 * gy01 + w11 * gy11);
+    s.gz = dz * gz;
+    return s;
+}
+
+template <int RY>
+struct Imm {  // a row stride known at compile time (immediate offsets)
+    __device__ __forceinline__ constexpr operator int() const { return RY; }
+};
+
+__device__ __noinline__ PlaneSample sample_global(const float* __restrict__ qt, int nx, int ny, int nz, int i, int j,
+                                                  float fx, float fy, int k)
+{
+    const int nyp = padded_ny(ny);
+    const size_t plane = padded_plane(nx, ny);
+    const int km = k > 0 ? k - 1 : k, kp = k + 1 < nz ? k + 1 : k;
+    const float dz = (k > 0 && k + 1 < nz) ? 0.5f : 1.f;
+    const size_t node = (size_t)(i + 1) * nyp + j + kPadY;
+    return sample_node(qt + (size_t)k * plane + node, qt + (size_t)km * plane + node, qt + (size_t)kp * plane + node,
+                       nyp, dz, fx, fy);
+}
+
+struct MarchConsts {
+    float ihx, ihy, ihz, hz;
+};
+
+struct MarchRay {
+    float u, v, tx, ty, ax, ay, e_prev, q0;
+    float phi, phi_c;  // Neumaier-compensated phase sum (per m)
+};
+
+__device__ __forceinline__ void march_accel(const PlaneSample& f, float sx, float sy, float q0, const MarchConsts& mc,
+                                            float& ax, float& ay)
+{
+    const float vv = 1.f + q0 - f.q;  // |v|^2 / c^2; the ray turns back where it reaches 0
+    const float c = -0.5f * (1.f + sx * sx + sy * sy) * rcp_approx(vv > 1e-6f ? vv : 1e-6f);
+    const float gz = f.gz * mc.ihz;
+    ax = c * (f.gx * mc.ihx - sx * gz);
+    ay = c * (f.gy * mc.ihy - sy * gz);
+}
+
+__device__ __forceinline__ float march_dphase(const PlaneSample& f, float sx, float sy)
+{
+    return index_minus_one(f.q) * sqrt_approx(1.f + sx * sx + sy * sy);
+}
+
+__device__ __forceinline__ void march_start(MarchRay& r, const PlaneSample& s, const MarchConsts& mc)
+{
+    r.q0 = s.q;
+    r.tx = r.ty = 0.f;
+    march_accel(s, 0.f, 0.f, r.q0, mc, r.ax, r.ay);
+    r.e_prev = march_dphase(s, 0.f, 0.f);
+    r.phi = r.phi_c = 0.f;
+}
+
+// First half of a step of h (m): half kick, then the drift to the next plane.
+__device__ __forceinline__ void march_kick_drift(MarchRay& r, float h, const MarchConsts& mc)
+{
+    const float hh = 0.5f * h;
+    r.tx = fmaf(hh, r.ax, r.tx);
+    r.ty = fmaf(hh, r.ay, r.ty);
+    r.u = fmaf(h * mc.ihx, r.tx, r.u);
+    r.v = fmaf(h * mc.ihy, r.ty, r.v);
+}
+
+// Second half: the closing half kick with the fields s on the new plane (its
+// slope-dependent term from a predictor), and the trapezoid phase of the step.
+__device__ __forceinline__ void march_kick(MarchRay& r, float h, const PlaneSample& s, const MarchConsts& mc)
+{
+    const float hh = 0.5f * h;
+    float bx, by;
+    march_accel(s, r.tx, r.ty, r.q0, mc, bx, by);
+    march_accel(s, fmaf(hh, bx, r.tx), fmaf(hh, by, r.ty), r.q0, mc, r.ax, r.ay);
+    r.tx = fmaf(hh, r.ax, r.tx);
+    r.ty = fmaf(hh, r.ay, r.ty);
+    const float e = march_dphase(s, r.tx, r.ty);
+    const float d = hh * (r.e_prev + e);
+    const float t = r.phi + d;
+    r.phi_c += fabsf(r.phi) >= fabsf(d) ? (r.phi - t) + d : (d - t) + r.phi;
+    r.phi = t;
+    r.e_prev = e;
+}
+
+__device__ __forceinline__ void march_write(const MarchRay& r, double k0, int n, int p, float* __restrict__ out)
+{
+    out[p] = atanf(r.tx);
+    out[n + p] = atanf(r.ty);
+    out[2 * n + p] = (float)(k0 * ((double)r.phi + (double)r.phi_c));
+}
+
+// Any pixel grid: one thread per ray, fields read from the padded q through L1/L2.
+__global__ void __launch_bounds__(128) march_kernel(const float* __restrict__ ws, size_t ws_field, int nx, int ny,
+                                                    int nz, MarchConsts mc, double k0, int P, float* __restrict__ out)
+{
+    const int n = P * P;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float* __restrict__ qt = ws + blockIdx.y * ws_field;
+    out += (size_t)blockIdx.y * 5 * n;
+    const int pi = p / P, pj = p % P;
+    MarchRay r;
+    r.u = (float)(((pi + 0.5) / P) * (nx - 1));
+    r.v = (float)(((pj + 0.5) / P) * (ny - 1));
+    for (int k = 0; k < nz; ++k) {
+        if (k > 0) march_kick_drift(r, mc.hz, mc);
+        int i, j;
+        float fx, fy;
+        PlaneSample s{0.f, 0.f, 0.f, 0.f};
+        if (locate(r.u, r.v, nx, ny, i, j, fx, fy)) s = sample_global(qt, nx, ny, nz, i, j, fx, fy, k);
+        if (k == 0)
+            march_start(r, s, mc);
+        else
+            march_kick(r, mc.hz, s, mc);
+    }
+    march_write(r, k0, n, p, out);
+}
+
+constexpr int kMarchCols = 32;  // rays per tile row (one warp)
+constexpr int kMarchRows = 8;   // tile rows (warps per block)
+constexpr int kMarchHalo = 8;
+constexpr int kMarchRing = 8;
+constexpr int kMarchRX = kMarchRows + 2 * kMarchHalo + 4;  // staged rows: tile span + halo + the 4-node stencil
+constexpr int kMarchRY = kMarchCols + 2 * kMarchHalo + 8;  // staged columns, incl. the 16-byte alignment slack
+constexpr int kMarchPlane = kMarchRX * kMarchRY;
+constexpr int kMarchChunks = kMarchPlane / 4;  // 16-byte chunks per staged plane
+constexpr int kMarchThreads = kMarchCols * kMarchRows;
+constexpr int kMarchChunksPerThread = (kMarchChunks + kMarchThreads - 1) / kMarchThreads;
+static_assert(kMarchRY % 4 == 0, "staged rows must be whole 16-byte chunks");
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+
+// Pixel grids at least as fine as the node grid (a tile spans at most
+// kMarchRows x kMarchCols node cells).  Window coordinates are padded ones:
+// row R = x + 1, column C = y + kPadY.
+__global__ void __launch_bounds__(kMarchThreads) march_staged_kernel(const float* __restrict__ ws, size_t ws_field,
+                                                                     int nx, int ny, int nz, MarchConsts mc, double k0,
+                                                                     int P, float* __restrict__ out)
+{
+    extern __shared__ __align__(16) float ring[];
+    const float* __restrict__ qt = ws + blockIdx.z * ws_field;
+    out += (size_t)blockIdx.z * 5 * P * P;
+    const int ti = threadIdx.x / kMarchCols, tj = threadIdx.x % kMarchCols;
+    const int pi = blockIdx.y * kMarchRows + ti, pj = blockIdx.x * kMarchCols + tj;
+    const bool active = pi < P && pj < P;
+    const int nyp = padded_ny(ny);
+    const size_t plane = padded_plane(nx, ny);
+    const double sxp = (double)(nx - 1) / P, syp = (double)(ny - 1) / P;
+    const int R0 = (int)floor((blockIdx.y * kMarchRows + 0.5) * sxp) + 1 - kMarchHalo;
+    const int C0 = ((int)floor((blockIdx.x * kMarchCols + 0.5) * syp) + kPadY - kMarchHalo) & ~3;
+    // staged rows/columns that exist in the padded plane
+    const int vR0 = max(R0, 0), vR1 = min(R0 + kMarchRX, nx + 2);
+    const int vC0 = max(C0, 0), vC1 = min(C0 + kMarchRY, nyp);
+    int soff[kMarchChunksPerThread];
+    long long goff[kMarchChunksPerThread];
+#pragma unroll
+    for (int q = 0; q < kMarchChunksPerThread; ++q) {
+        const int c = threadIdx.x + q * kMarchThreads;
+        soff[q] = -1;
+        goff[q] = 0;
+        if (c < kMarchChunks) {
+            const int r = c / (kMarchRY / 4), cc = (c % (kMarchRY / 4)) * 4;
+            const int R = R0 + r, C = C0 + cc;
+            if (R >= 0 && R < nx + 2 && C >= 0 && C + 4 <= nyp) {
+                soff[q] = r * kMarchRY + cc;
+                goff[q] = (long long)R * nyp + C;
+            }
+        }
+    }
+    auto issue = [&](int pl) {
+        if (pl < nz) {
+            float* dst = ring + (pl & (kMarchRing - 1)) * kMarchPlane;
+            const float* src = qt + (size_t)pl * plane;
+#pragma unroll
+            for (int q = 0; q < kMarchChunksPerThread; ++q)
+                if (soff[q] >= 0) cp_async16(dst + soff[q], src + goff[q]);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+
+    for (int pl = 0; pl < kMarchRing - 2; ++pl) issue(pl);
+    MarchRay r;
+    r.u = (float)(((pi + 0.5) / P) * (nx - 1));
+    r.v = (float)(((pj + 0.5) / P) * (ny - 1));
+    for (int k = 0; k < nz; ++k) {
+        // planes k-1..k+1 must be in the ring: all but the newest kMarchRing - 4 groups done
+        asm volatile("cp.async.wait_group %0;" ::"n"(kMarchRing - 4) : "memory");
+        __syncthreads();
+        issue(k + kMarchRing - 2);  // into the slot of plane k - 2, which no step reads any more
+        if (!active) continue;
+        if (k > 0) march_kick_drift(r, mc.hz, mc);
+        int i, j;
+        float fx, fy;
+        PlaneSample s{0.f, 0.f, 0.f, 0.f};
+        if (locate(r.u, r.v, nx, ny, i, j, fx, fy)) {
+            // stencil rows x = i-1..i+2 -> R = i..i+3, columns y = j-1..j+2 -> C = j+kPadY-1..j+kPadY+2
+            const int R = i + 1, C = j + kPadY;
+            if (R - 1 >= vR0 && R + 2 < vR1 && C - 1 >= vC0 && C + 2 < vC1) {
+                const int km = k > 0 ? k - 1 : k, kp = k + 1 < nz ? k + 1 : k;
+                const float dz = (k > 0 && k + 1 < nz) ? 0.5f : 1.f;
+                const int b = (R - R0) * kMarchRY + (C - C0);
+                s = sample_node(ring + (k & (kMarchRing - 1)) * kMarchPlane + b,
+                                ring + (km & (kMarchRing - 1)) * kMarchPlane + b,
+                                ring + (kp & (kMarchRing - 1)) * kMarchPlane + b, Imm<kMarchRY>{}, dz, fx, fy);
+            } else {
+                s = sample_global(qt, nx, ny, nz, i, j, fx, fy, k);
+            }
+        }
+        if (k == 0)
+            march_start(r, s, mc);
+        else
+            march_kick(r, mc.hz, s, mc);
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (active) march_write(r, k0, P * P, pi * P + pj, out);
+}
+
+}  // namespace
+
+extern "C" size_t tt_march_maps_batched_workspace_bytes(int nfields, int nx, int ny, int nz)
+{
+    if (nfields < 1 || nx < 2 || ny < 2 || nz < 2) return 0;
+    return (size_t)nfields * field_ws_floats(nx, ny, nz) * sizeof(float);
+}
+
+extern "C" size_t tt_march_maps_workspace_bytes(int nx, int ny, int nz)
+{
+    return tt_march_maps_batched_workspace_bytes(1, nx, ny, nz);
+}
+
+extern "C" int tt_march_maps_batched(const void* const* ne, int nfields, int ne_dtype, int nx, int ny, int nz,
+                                     const double* x, const double* y, const double* z, double lwl, double ne_max,
+                                     int P, float* out, void* workspace, size_t workspace_bytes, void* stream)
+{
+    if (!ne || !x || !y || !z || !out || !workspace) return tt::invalid("march_maps: NULL pointer");
+    if (nfields < 1 || nfields > TT_MAX_MARCH_FIELDS) return tt::invalid("march_maps: 1..TT_MAX_MARCH_FIELDS fields");
+    if (nx < 2 || ny < 2 || nz < 2 || P < 1 || (long long)P * P > 0x7fffffffLL / 5 || nx > 65535 || ny > 65535 * 32)
+        return tt::invalid("march_maps: bad sizes");
+    if (workspace_bytes < tt_march_maps_batched_workspace_bytes(nfields, nx, ny, nz))
+        return tt::invalid("march_maps: workspace too small");
+    if (ne_dtype != TT_F32 && ne_dtype != TT_F64) return tt::invalid("march_maps: ne_dtype");
+    if ((reinterpret_cast<uintptr_t>(workspace) & 15) != 0) return tt::invalid("march_maps: workspace not 16-byte aligned");
+    MarchFields fields{};
+    for (int f = 0; f < nfields; ++f) {
+        if (!ne[f]) return tt::invalid("march_maps: NULL field");
+        fields.ne[f] = ne[f];
+    }
+    const double hx = (x[nx - 1] - x[0]) / (nx - 1), hy = (y[ny - 1] - y[0]) / (ny - 1),
+                 hz = (z[nz - 1] - z[0]) / (nz - 1);
+    if (!(hx > 0) || !(hy > 0) || !(hz > 0)) return tt::invalid("march_maps: coordinates must increase");
+    const double omega = 2.0 * CUDART_PI * (TT_C_LIGHT / lwl);
+    const double nc = 3.14207787e-4 * omega * omega;
+    const double k0 = omega / TT_C_LIGHT;
+    cudaStream_t s = tt::as_stream(stream);
+    float* ws = static_cast<float*>(workspace);
+    const size_t wsf = field_ws_floats(nx, ny, nz);
+    const dim3 tg((ny + 31) / 32, nx, nfields);
+    if (ne_dtype == TT_F32)
+        plane_q_kernel<float><<<tg, 256, 0, s>>>(fields, nx, ny, nz, (float)(1.0 / nc), (float)ne_max, ws, wsf);
+    else
+        plane_q_kernel<double><<<tg, 256, 0, s>>>(fields, nx, ny, nz, (float)(1.0 / nc), (float)ne_max, ws, wsf);
+    TT_TRY(tt::launch_status("march_maps plane_q"));
+    const long long nghost = (2LL * nx + 2LL * ny) * nz * nfields;
+    plane_ghost_kernel<<<(unsigned)((nghost + 255) / 256), 256, 0, s>>>(nfields, nx, ny, nz, ws, wsf);
+    TT_TRY(tt::launch_status("march_maps ghost"));
+    const int n = P * P;
+    straight_from_colsum_kernel<<<dim3((n + 255) / 256, nfields), 256, 0, s>>>(
+        ws, wsf, nx, ny, nz, (float)(-0.5 * hz / hx), (float)(-0.5 * hz / hy), P, out);
+    TT_TRY(tt::launch_status("march_maps straight"));
+    const MarchConsts mc{(float)(1.0 / hx), (float)(1.0 / hy), (float)(1.0 / hz), (float)hz};
+    // staged tiles need a tile to span at most kMarchRows x kMarchCols node cells
+    if ((long long)(nx - 1) <= P && (long long)(ny - 1) <= P) {
+        const size_t smem = (size_t)kMarchRing * kMarchPlane * sizeof(float);
+        TT_TRY(tt::cuda_status(cudaFuncSetAttribute(march_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)smem),
+                               "march_maps attribute"));
+        const dim3 grid((P + kMarchCols - 1) / kMarchCols, (P + kMarchRows - 1) / kMarchRows, nfields);
+        march_staged_kernel<<<grid, kMarchThreads, smem, s>>>(ws, wsf, nx, ny, nz, mc, k0, P, out);
+    } else {
+        march_kernel<<<dim3((n + 127) / 128, nfields), 128, 0, s>>>(ws, wsf, nx, ny, nz, mc, k0, P, out);
+    }
+    return tt::launch_status("march_maps");
+}
+
+extern "C" int tt_march_maps(const void* ne, int ne_dtype, int nx, int ny, int nz, const double* x, const double* y,
+                             const double* z, double lwl, double ne_max, int P, float* out, void* workspace,
+                             size_t workspace_bytes, void* stream)
+{
+    const void* one[1] = {ne};
+    return tt_march_maps_batched(one, 1, ne_dtype, nx, ny, nz, x, y, z, lwl, ne_max, P, out, workspace,
+                                 workspace_bytes, stream);
 }
 
 // Geometric-optics shadowgram of a deflection map: rays leaving pixel centres

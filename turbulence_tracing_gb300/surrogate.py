@@ -1,30 +1,37 @@
 """Learned surrogate with exact-tracer fallback.
 
-Task: from the straight-line (unbent-ray) path integrals of a density field,
-predict what the full trace gives -- the deflection of each pixel-centre ray
-and its phase -- and fall back to the exact FP32 tracer where the network's
-own error estimate says the prediction would miss.
+Task: from path integrals of a density field, predict what the full trace
+gives -- the exit deflection of each pixel-centre ray and its phase -- and fall
+back to the exact FP32 tracer where the network's own error estimate says the
+prediction would miss.
 
-Per realisation (an S^3 field of side L, drawn like the batched ensemble):
-  maps     tt_straight_line_maps: straight-line deflection (2 maps) and phase
-           of the S x S pixel-centre rays -- the method without the network --
-           and the deflection accumulated in each of nslab slabs along the
-           path (2 maps per slab)
-  inputs   the deflection maps (total and per slab) / s, s the rms of the
-           total deflection, and a constant map log10(s (S - 1)) -- the
-           straight-line drift across the box in cells, i.e. how far into the
-           nonlinear regime the field is
-  targets  (full-trace deflection - straight-line deflection) / (s^2 (S - 1))
-           and (full-trace phase - straight-line phase) / (k0 L s^2): both
-           corrections are second order in the field, so these are O(1)
-           from weak to strong fields
-  network  the FNO of fno.py (4 layers, width 32, 16 modes), trained by the
-           library's own forward/backward kernels and Adam, one CUDA graph
-           per step
+Per realisation (an S^3 field of side L, drawn like the batched ensemble),
+one pass of tt_march_maps over the density gives
+  march     the S x S pixel-centre rays marched one node plane per step
+            through the ray equation (second order, one field sample per
+            cell): deflection (2 maps) and phase -- the coarse answer the
+            network corrects
+  straight  the straight-line deflection of the same rays -- the first-order
+            answer (tt_straight_line_maps' definition)
+and from those
+  inputs    straight and marched deflections / s, the marched phase
+            standardised over the field, and a constant map log10(s (S - 1)),
+            s the rms straight deflection: the straight-line drift across the
+            box in cells, i.e. how far into the nonlinear regime the field is
+  targets   (full-trace - marched deflection) / s and
+            (full-trace - marched phase) / (k0 L s^2), each channel scaled to
+            unit rms over the training set (Workload.gain, fixed by the first
+            dataset built and used for every later one)
+  network   the FNO of fno.py (4 layers, width 32, 16 modes), trained by the
+            library's own forward/backward kernels and Adam, one CUDA graph
+            per step
+Why the march: once rays drift by a cell or more, the full trace samples the
+field off the straight path, which a projection along z does not record; the
+straight-line maps alone then leave most of the shadowgram error in place.
 Shadowgram intensity comes from tt_shadowgram (geometric optics, drift D set
 per field from the straight-line map so the contrast is 20%); the error of a
 prediction is ||I_pred - I_trace||_2 / ||I_trace||_2.  The error estimate is
-kappa * ||I_net - I_straight|| / ||I_net|| (how far the network moved the
+kappa * ||I_net - I_march|| / ||I_net|| (how far the network moved the
 answer), kappa calibrated on held-out fields so that 90% of them are bounded.
 """
 import math
@@ -45,15 +52,18 @@ def draw_fields(n, seed=0, exponents=(-5.0 / 3.0, -3.0, -11.0 / 3.0), delta=(0.0
                  ne0=float(rng.uniform(*ne0)), seed=int(rng.integers(0, 2 ** 62))) for _ in range(n)]
 
 
-class Workload:
-    """Fields, straight-line maps, exact traces and shadowgrams at one grid size."""
+IN_CHANNELS = 6
+N_MAPS = 5  # tt_march_maps: marched (theta_x, theta_y, phase), then straight (theta_x, theta_y)
 
-    def __init__(self, S, L=2e-3, lwl=1064e-9, rtol=1e-7, contrast=0.2, nslab=4):
+
+class Workload:
+    """Fields, straight-line and marched maps, exact traces and shadowgrams at one grid size."""
+
+    def __init__(self, S, L=2e-3, lwl=1064e-9, rtol=1e-7, contrast=0.2):
         self.dev = core.require_cuda()
         self.S, self.L, self.lwl, self.rtol, self.contrast = S, L, lwl, rtol, contrast
-        self.nslab = nslab
-        self.in_ch = in_channels(nslab)
-        self.n_maps = 3 + 2 * nslab
+        self.in_ch = IN_CHANNELS
+        self.n_maps = N_MAPS
         self.x = np.linspace(-L / 2, L / 2, S)
         self.ext = float(self.x.max())
         self.t_end = float(np.linspace(0.0, math.sqrt(8.0) * self.ext / C_LIGHT, 2)[-1])
@@ -67,12 +77,21 @@ class Workload:
         self.s0 = torch.as_tensor(s0, device=self.dev)
         self.vol = None
         self.trace_out = None
+        self.march_ws = None
+        self.gain = None  # per-channel target scale (3,), set from the first dataset
 
     def field(self, p):
         return core.grf_field(self.S, self.L, p["alpha"], p["ne0"], p["delta"], p["seed"], dtype=torch.float32)
 
     def maps(self, ne, out=None):
-        return core.straight_line_maps(ne, self.x, self.x, self.x, self.S, lwl=self.lwl, out=out, nslab=self.nslab)
+        """Straight-line maps alone (tt_straight_line_maps): deflection (2) and phase."""
+        return core.straight_line_maps(ne, self.x, self.x, self.x, self.S, lwl=self.lwl, out=out)
+
+    def march(self, ne, out=None):
+        """Marched and straight-line maps from one pass (5, S, S)."""
+        if self.march_ws is None:
+            self.march_ws = torch.empty(core.march_workspace_bytes(ne.shape), dtype=torch.uint8, device=self.dev)
+        return core.march_maps(ne, self.x, self.x, self.x, self.S, lwl=self.lwl, out=out, ws=self.march_ws)
 
     def trace(self, ne):
         """Exact FP32 trace of the pixel-centre rays: (theta (2,S,S) f32, phase (S,S) f64, steps tensor)."""
@@ -88,43 +107,50 @@ class Workload:
         return theta, o["phase"].view(S, S), o["nsteps"].sum()
 
     def drift(self, straight):
-        """Free drift D (m) giving the straight-line map the set shadowgram contrast."""
+        """Free drift D (m, device scalar) giving the straight-line map the set shadowgram contrast."""
         _, div = core.shadowgram(straight[0:2].contiguous(), self.pitch, 0.0, want_intensity=False, want_div=True)
         return self.contrast / torch.sqrt((div.double() ** 2).mean())
 
-    def shadow(self, theta, D):
-        return core.shadowgram(theta.contiguous(), self.pitch, float(D))[0]
+    def shadow(self, theta, D, out=None):
+        return core.shadowgram(theta.contiguous(), self.pitch, float(D), intensity=out)[0]
 
 
-def in_channels(nslab):
-    return 3 + 2 * nslab
+def encode_batch(mm, S, out):
+    """Network inputs out (n, 6, S, S) and the scales s (n,) from march outputs
+    mm (n, 5, S, S): straight and marched deflections / s, the marched phase
+    standardised per field, log10 of the straight-line drift in cells."""
+    s = torch.sqrt((mm[:, 3:5].double() ** 2).mean(dim=(1, 2, 3))).float().clamp_min(1e-30)
+    sb = s[:, None, None, None]
+    out[:, 0:2] = mm[:, 3:5] / sb
+    out[:, 2:4] = mm[:, 0:2] / sb
+    ph = mm[:, 2].double()
+    mu = ph.mean(dim=(1, 2), keepdim=True)
+    sd = ph.std(dim=(1, 2), keepdim=True).clamp_min(1e-30)
+    out[:, 4] = ((ph - mu) / sd).float()
+    out[:, 5] = torch.log10(s * (S - 1))[:, None, None]
+    return s
 
 
-def encode(maps, S):
-    """Network input (3 + 2 nslab, S, S) and the scale s from straight-line maps
-    (3 + 2 nslab, S, S): total and slab deflections / s, then log10 drift."""
-    nin = maps.shape[0]
-    s = torch.sqrt((maps[0:2].double() ** 2).mean()).float().clamp_min(1e-30)
-    inp = torch.empty((nin, S, S), dtype=torch.float32, device=maps.device)
-    inp[0:2] = maps[0:2] / s
-    inp[2:nin - 1] = maps[3:nin] / s
-    inp[nin - 1] = torch.log10(s * (S - 1))
-    return inp, s
+def encode(mm, S, k0, L, out=None):
+    """Network input (6, S, S) and the scale s (device scalar) for one field."""
+    inp = torch.empty((IN_CHANNELS, S, S), dtype=torch.float32, device=mm.device) if out is None else out
+    s = encode_batch(mm[None], S, inp[None])
+    return inp, s[0]
 
 
-def targets(maps, theta, phase, s, k0, L):
-    S = maps.shape[-1]
-    t = torch.empty((3, S, S), dtype=torch.float32, device=maps.device)
-    t[0:2] = (theta - maps[0:2]) / (s * s * (S - 1))
-    t[2] = ((phase - maps[2].double()) / (k0 * L * s.double() ** 2)).float()
+def targets(march, theta, phase, s, k0, L):
+    """Unscaled targets (3, S, S): the full trace's departure from the march."""
+    S = march.shape[-1]
+    t = torch.empty((3, S, S), dtype=torch.float32, device=march.device)
+    t[0:2] = (theta - march[0:2]) / s
+    t[2] = ((phase - march[2].double()) / (k0 * L * s.double() ** 2)).float()
     return t
 
 
-def decode(out, maps, s, k0, L):
+def decode(out, march, s, k0, L, gain):
     """Predicted deflection (2, S, S) and phase (S, S) from network output (3, S, S)."""
-    S = maps.shape[-1]
-    theta = maps[0:2] + (s * s * (S - 1)) * out[0:2]
-    phase = maps[2].double() + (k0 * L) * s.double() ** 2 * out[2].double()
+    theta = march[0:2] + (s / gain[0:2, None, None]) * out[0:2]
+    phase = march[2].double() + (k0 * L) * s.double() ** 2 * (out[2] / gain[2]).double()
     return theta, phase
 
 
@@ -133,29 +159,35 @@ def rel_l2(a, b):
 
 
 def build_dataset(W, params, keep_truth=False):
-    """Inputs and targets (N, 3, S, S) on the device; optionally the straight-line
-    maps, exact deflections and phases for evaluation."""
+    """Inputs and targets (N, 3, S, S) on the device; optionally the marched and
+    straight-line maps, exact deflections and phases for evaluation."""
     N, S = len(params), W.S
     X = torch.empty((N, W.in_ch, S, S), dtype=torch.float32, device=W.dev)
     Y = torch.empty((N, 3, S, S), dtype=torch.float32, device=W.dev)
     scale = torch.empty(N, dtype=torch.float32, device=W.dev)
     truth = None
     if keep_truth:
-        truth = {"maps": torch.empty((N, W.n_maps, S, S), dtype=torch.float32, device=W.dev), "theta": torch.empty((N, 2, S, S), dtype=torch.float32, device=W.dev),
+        truth = {"march": torch.empty((N, W.n_maps, S, S), dtype=torch.float32, device=W.dev),
+                 "straight_phase": torch.empty((N, S, S), dtype=torch.float32, device=W.dev),
+                 "theta": torch.empty((N, 2, S, S), dtype=torch.float32, device=W.dev),
                  "phase": torch.empty((N, S, S), dtype=torch.float64, device=W.dev)}
     steps = torch.zeros((), dtype=torch.int64, device=W.dev)
     for i, p in enumerate(params):
         ne = W.field(p)
-        m = W.maps(ne)
+        mm = W.march(ne)
         theta, phase, st = W.trace(ne)
-        X[i], s = encode(m, S)
+        _, s = encode(mm, S, W.k0, W.L, out=X[i])
         scale[i] = s
-        Y[i] = targets(m, theta, phase, s, W.k0, W.L)
+        Y[i] = targets(mm, theta, phase, s, W.k0, W.L)
         steps += st
         if keep_truth:
-            truth["maps"][i] = m
+            truth["march"][i] = mm
+            truth["straight_phase"][i] = W.maps(ne)[2]
             truth["theta"][i] = theta
             truth["phase"][i] = phase
+    if W.gain is None:
+        W.gain = (1.0 / torch.sqrt((Y.double() ** 2).mean(dim=(0, 2, 3))).clamp_min(1e-30)).float()
+    Y *= W.gain[None, :, None, None]
     return X, Y, scale, truth, steps
 
 
@@ -233,23 +265,28 @@ def predict(net, X, batch=8):
 
 
 def evaluate(W, net, X, scale, truth, batch=8):
-    """Per-field shadowgram errors of the straight-line map, the network and the
-    network's own correction size (the basis of its error estimate)."""
+    """Per-field shadowgram errors of the straight-line map, the march and the
+    network, and the network's own correction size (the basis of its error
+    estimate)."""
     out = predict(net, X, batch)
     res = []
     for i in range(X.shape[0]):
-        m = truth["maps"][i]
+        mm = truth["march"][i]
+        m = torch.cat([mm[3:5], truth["straight_phase"][i][None]])
+        th_t, ph_t = truth["theta"][i], truth["phase"][i]
         D = W.drift(m)
-        th_net, ph_net = decode(out[i], m, scale[i], W.k0, W.L)
-        I_t = W.shadow(truth["theta"][i], D)
+        th_net, ph_net = decode(out[i], mm, scale[i], W.k0, W.L, W.gain)
+        I_t = W.shadow(th_t, D)
         I_s = W.shadow(m[0:2], D)
+        I_m = W.shadow(mm[0:2], D)
         I_n = W.shadow(th_net, D)
-        res.append({"err_straight": rel_l2(I_s, I_t), "err_net": rel_l2(I_n, I_t), "moved": rel_l2(I_n, I_s) *
-                    float(torch.linalg.norm(I_s.double()) / torch.linalg.norm(I_n.double())),
-                    "theta_err_straight": rel_l2(m[0:2], truth["theta"][i]),
-                    "theta_err_net": rel_l2(th_net, truth["theta"][i]),
-                    "phase_corr_err_net": float(torch.linalg.norm(ph_net - truth["phase"][i]) /
-                                                torch.linalg.norm(truth["phase"][i] - m[2].double())),
+        corr = torch.linalg.norm(ph_t - m[2].double())
+        res.append({"err_straight": rel_l2(I_s, I_t), "err_march": rel_l2(I_m, I_t), "err_net": rel_l2(I_n, I_t),
+                    "moved": rel_l2(I_n, I_m) * float(torch.linalg.norm(I_m.double()) / torch.linalg.norm(I_n.double())),
+                    "theta_err_straight": rel_l2(m[0:2], th_t), "theta_err_march": rel_l2(mm[0:2], th_t),
+                    "theta_err_net": rel_l2(th_net, th_t),
+                    "phase_corr_err_march": float(torch.linalg.norm(mm[2].double() - ph_t) / corr),
+                    "phase_corr_err_net": float(torch.linalg.norm(ph_net - ph_t) / corr),
                     "log_drift": float(X[i, -1, 0, 0])})
     return res
 
@@ -261,52 +298,94 @@ def calibrate(res, quantile=0.9):
 
 
 class Pipeline:
-    """Surrogate with fallback: for each field, straight-line maps -> network ->
-    shadowgram and error estimate; fields whose estimate exceeds tol are traced."""
+    """Surrogate with fallback, a chunk of fields at a time: one batched march
+    over the chunk (marched and straight-line maps) -> network -> shadowgrams
+    and error estimates, all on the device with one host read per chunk (the
+    estimates); the fields whose estimate exceeds tol are traced exactly.  The
+    detector drift D of each field is part of its detector set-up (given)."""
 
     def __init__(self, W, net, kappa, tol=0.02, batch=8):
         self.W, self.net, self.kappa, self.tol, self.B = W, net, kappa, tol, batch
-        S = W.S
-        self.X = torch.empty((batch, W.in_ch, S, S), dtype=torch.float32, device=W.dev)
-        self.out = torch.empty((batch, 3, S, S), dtype=torch.float32, device=W.dev)
-        self.maps = torch.empty((batch, W.n_maps, S, S), dtype=torch.float32, device=W.dev)
+        S, dev = W.S, W.dev
+        self.X = torch.empty((batch, W.in_ch, S, S), dtype=torch.float32, device=dev)
+        self.out = torch.empty((batch, 3, S, S), dtype=torch.float32, device=dev)
+        self.mar = torch.empty((batch, W.n_maps, S, S), dtype=torch.float32, device=dev)
+        self.theta = torch.empty((batch, 2, S, S), dtype=torch.float32, device=dev)
+        self.I = torch.empty((batch, 2, S, S), dtype=torch.float32, device=dev)
+        self.ws = None
 
-    def run(self, fields):
-        """fields: list of density tensors.  Returns (intensity list, fell_back list)."""
+    def run(self, fields, Ds):
+        """fields: list of density tensors, Ds: their drifts.  Returns
+        (intensity list, fell_back list)."""
         W, S = self.W, self.W.S
         I_out, fell = [], []
         for b0 in range(0, len(fields), self.B):
-            chunk = fields[b0:b0 + self.B]
+            chunk, D = fields[b0:b0 + self.B], Ds[b0:b0 + self.B]
             n = len(chunk)
-            sc = []
-            for i, ne in enumerate(chunk):
-                W.maps(ne, out=self.maps[i])
-                self.X[i], s = encode(self.maps[i], S)
-                sc.append(s)
-            self.net.forward(self.X, out=self.out)
+            if self.ws is None:
+                need = core.march_batched_workspace_bytes(self.B, chunk[0].shape)
+                self.ws = torch.empty(need, dtype=torch.uint8, device=W.dev)
+            core.march_maps_batched(chunk, W.x, W.x, W.x, S, lwl=W.lwl, out=self.mar[:n], ws=self.ws)
+            s = encode_batch(self.mar[:n], S, self.X[:n])
+            if n == self.B:
+                self.net.forward(self.X, out=self.out)
+            else:
+                self.out[:n] = self.net.forward(self.X[:n].contiguous())
+            self.theta[:n] = self.mar[:n, 0:2] + (s[:, None, None, None] / W.gain[None, 0:2, None, None]) * \
+                self.out[:n, 0:2]
             for i in range(n):
-                m = self.maps[i]
-                D = W.drift(m)
-                th, _ = decode(self.out[i], m, sc[i], W.k0, W.L)
-                I_n = W.shadow(th, D)
-                I_s = W.shadow(m[0:2], D)
-                est = self.kappa * rel_l2(I_n, I_s) * float(torch.linalg.norm(I_s.double()) /
-                                                            torch.linalg.norm(I_n.double()))
-                if est > self.tol:
+                W.shadow(self.theta[i], D[i], out=self.I[i, 0])
+                W.shadow(self.mar[i, 0:2], D[i], out=self.I[i, 1])
+            In, Im = self.I[:n, 0].double(), self.I[:n, 1].double()
+            est = (self.kappa * torch.linalg.norm(In - Im, dim=(1, 2)) / torch.linalg.norm(In, dim=(1, 2))).tolist()
+            for i in range(n):
+                if est[i] > self.tol:
                     theta, _, _ = W.trace(chunk[i])
-                    I_n = W.shadow(theta, D)
+                    I_out.append(W.shadow(theta, D[i]))
                     fell.append(True)
                 else:
+                    I_out.append(self.I[i, 0].clone())
                     fell.append(False)
-                I_out.append(I_n)
         return I_out, fell
 
-    def run_tracer(self, fields):
-        """The exact method alone: trace every field."""
+    def run_tracer(self, fields, Ds):
+        """The exact method alone: trace every field, one field per launch."""
         out = []
-        for ne in fields:
-            m = self.W.maps(ne)
-            D = self.W.drift(m)
+        for ne, D in zip(fields, Ds):
             theta, _, _ = self.W.trace(ne)
             out.append(self.W.shadow(theta, D))
         return out
+
+
+class BatchedTracer:
+    """The exact method at its best throughput: a chunk of fields traced in one
+    batched persistent launch (tt_trace_f32_batched), then their shadowgrams."""
+
+    def __init__(self, W, batch=8):
+        self.W, self.B = W, batch
+        self.vols = [None] * batch
+        self.s0 = W.s0.reshape(-1).repeat(batch)
+        self.out = None
+
+    def run(self, fields, Ds):
+        W, S = self.W, self.W.S
+        res = []
+        for b0 in range(0, len(fields), self.B):
+            chunk, D = fields[b0:b0 + self.B], Ds[b0:b0 + self.B]
+            n = len(chunk)
+            for i, ne in enumerate(chunk):
+                v = self.vols[i]
+                self.vols[i] = core.build_volume(ne, W.x, W.x, W.x, 2, lwl=W.lwl,
+                                                 nodes=None if v is None else v.nodes)
+            offs = [S * S * i for i in range(n + 1)]
+            if self.out is not None and n != self.B:
+                self.out = None
+            o = core.trace_f32_batched(self.vols[:n], self.s0[:6 * S * S * n], offs, [W.t_end] * n, [W.ext] * n,
+                                       rtol=W.rtol, phase=True, want_sf=False,
+                                       ws=None if self.out is None else self.out["_ws"], out=self.out)
+            self.out = o if n == self.B else None
+            for i in range(n):
+                rf = core.ray_block(o["rf"], 4, offs, i)
+                theta = torch.stack([rf[1].view(S, S), rf[3].view(S, S)]).float()
+                res.append(W.shadow(theta, D[i]))
+        return res

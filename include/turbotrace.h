@@ -320,6 +320,10 @@ int tt_march_maps_batched(const void* const* ne, int nfields, int ne_dtype, int 
  * of D m, and div [P][P] = d theta_x/dx + d theta_y/dy (either output may be
  * NULL); differences central inside, one-sided at the edges. */
 int tt_shadowgram(const float* theta, int P, double pitch, double D, float* intensity, float* div, void* stream);
+/* tt_shadowgram's intensity for nmaps maps at once: theta FP32 [nmaps][2][P][P],
+ * D a device array of nmaps drifts (m), intensity FP32 [nmaps][P][P]. */
+int tt_shadowgram_batched(const float* theta, int nmaps, int P, double pitch, const double* D, float* intensity,
+                          void* stream);
 
 /* ---- Learned surrogate: 2D Fourier neural operator ----------------------------
  * No reference interface: the reference has no surrogate.  The network maps

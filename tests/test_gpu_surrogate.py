@@ -34,8 +34,9 @@ def _maps_restated(ne, x, lwl, S):
 def _march_restated(ne, x, lwl, P):
     """The plane march in float64: q = min(ne/n_c, 1), numpy.gradient
     derivatives, bilinear on the node planes (zero outside the grid), and
-    kick-drift-kick in z from plane to plane on the ray equation with the
-    second kick's slope-dependent term iterated once; trapezoid phase in ds.
+    kick-drift-kick in z from plane to plane on the ray equation, the closing
+    kick's slope-dependent term at the slope predicted with the previous
+    step's acceleration; trapezoid phase in ds.
     Then the straight ray from the same pixel centre: trapezoid deflection
     integrals on the planes."""
     omega, nc = R.critical_density(lwl)
@@ -76,8 +77,7 @@ def _march_restated(ne, x, lwl, P):
         tx, ty = tx + d / 2 * ax, ty + d / 2 * ay
         u, v = u + tx, v + ty
         f = sample(u, v, k)
-        bx, by = accel(f, tx, ty, q0)
-        ax, ay = accel(f, tx + d / 2 * bx, ty + d / 2 * by, q0)
+        ax, ay = accel(f, tx + d / 2 * ax, ty + d / 2 * ay, q0)
         tx, ty = tx + d / 2 * ax, ty + d / 2 * ay
         e2 = dphase(f, tx, ty)
         phi += d / 2 * (e + e2)

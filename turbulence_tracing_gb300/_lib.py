@@ -130,6 +130,7 @@ SIGNATURES = {
     "tt_march_maps": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_double_p, c_double_p, c_double_p,
                               ctypes.c_double, ctypes.c_double, c_int, c_void_p, c_void_p, c_size, c_void_p]),
     "tt_shadowgram": (c_int, [c_void_p, c_int, ctypes.c_double, ctypes.c_double, c_void_p, c_void_p, c_void_p]),
+    "tt_shadowgram_batched": (c_int, [c_void_p, c_int, c_int, ctypes.c_double, c_void_p, c_void_p, c_void_p]),
     "tt_fno_param_count": (c_size, [ctypes.POINTER(TTFnoDims)]),
     "tt_fno_workspace_bytes": (c_size, [ctypes.POINTER(TTFnoDims), c_int]),
     "tt_fno_forward": (c_int, [ctypes.POINTER(TTFnoDims), c_void_p, c_void_p, c_void_p, c_void_p, c_size, c_void_p]),

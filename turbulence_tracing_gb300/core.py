@@ -415,6 +415,18 @@ def shadowgram(theta, pitch, D, intensity=None, div=None, want_intensity=True, w
     return (intensity if want_intensity else None), (div if want_div else None)
 
 
+def shadowgram_batched(theta, pitch, D, intensity=None):
+    """Intensities (n, P, P) of n deflection maps theta (n, 2, P, P) float32 with
+    drifts D (n,) float64 on the device (tt_shadowgram_batched)."""
+    dev = require_cuda()
+    n, P = theta.shape[0], theta.shape[-1]
+    if intensity is None:
+        intensity = torch.empty((n, P, P), dtype=torch.float32, device=dev)
+    check(_lib.lib().tt_shadowgram_batched(_ptr(theta), n, P, float(pitch), _ptr(D), _ptr(intensity), _stream()),
+          "tt_shadowgram_batched")
+    return intensity
+
+
 def grf_field(n, L_box, alpha, ne0, delta, seed, dtype=torch.float32, kmin=None, kmax=None):
     """Band-limited unit-variance GRF density ne0 (1 + delta g) clipped >= 0, (n, n, n)."""
     dev = require_cuda()

@@ -185,9 +185,10 @@ extern "C" int tt_straight_line_maps(const void* ne, int ne_dtype, int nx, int n
 //   dphi/dz = k0 (sqrt(1 - q) - 1) sqrt(1 + |t|^2)
 // (from dx/dt = v, dv/dt = -c^2/2 grad q and |v|^2 = c^2 (1 + q0 - q), q0 the
 // value at the entry point), stepped from node plane to node plane (step hz)
-// by kick-drift-kick with the second kick's slope-dependent term iterated once
-// (second order), the phase summed in FP32 with Neumaier compensation.  Every
-// plane is visited: skipping planes aliases the grid-scale gradient (the
+// by kick-drift-kick, the closing kick's slope-dependent term evaluated at the
+// slope predicted from the previous step's acceleration (second order), the
+// phase summed in FP32 with Kahan compensation (every term has the sign of
+// n - 1 <= 0).  Every plane is visited: skipping planes aliases the grid-scale gradient (the
 // trapezoid rule on a field with power at the node spacing).  On a plane the
 // fields are bilinear in x, y of the node values -- q and its numpy.gradient
 // derivatives, zero outside the grid, i.e. the tracer's trilinear fields
@@ -230,49 +231,91 @@ inline size_t field_ws_floats(int nx, int ny, int nz)
     return (f + 63) & ~(size_t)63;  // 256-byte aligned per field
 }
 
+// Four consecutive z values of column (a, y) from z on, zero past nz; VEC:
+// 16-byte aligned vector loads (nz % 4 == 0 and an aligned base).
+template <bool VEC>
+__device__ __forceinline__ void load4(const float* __restrict__ col, int z, int nz, float (&v)[4])
+{
+    if (VEC && z + 3 < nz) {
+        const float4 t = __ldg(reinterpret_cast<const float4*>(col + z));
+        v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = z + j < nz ? __ldg(col + z + j) : 0.f;
+    }
+}
+
+template <bool VEC>
+__device__ __forceinline__ void load4(const double* __restrict__ col, int z, int nz, float (&v)[4])
+{
+    if (VEC && z + 3 < nz) {
+        const double2 t0 = __ldg(reinterpret_cast<const double2*>(col + z));
+        const double2 t1 = __ldg(reinterpret_cast<const double2*>(col + z + 2));
+        v[0] = (float)t0.x, v[1] = (float)t0.y, v[2] = (float)t1.x, v[3] = (float)t1.y;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = z + j < nz ? (float)__ldg(col + z + j) : 0.f;
+    }
+}
+
 // q -> padded plane-major, and the trapezoid column sums Sum_k w_k q(x, y, k).
-// Block: one x, 32 columns y of field blockIdx.z; loops over z in tiles of 32
-// through shared memory (read along z, write along y).
-template <typename T>
+// Block: one x, 32 columns y of field blockIdx.z; z in chunks of 128 through
+// shared memory (read along z, four values a lane, 16 in flight a thread;
+// write along y).  The column sums are per-thread partials over the lane's z
+// values, reduced across the warp at the end (a fixed order).
+template <typename T, bool VEC>
 __global__ void __launch_bounds__(256) plane_q_kernel(const __grid_constant__ MarchFields fields, int nx, int ny,
                                                      int nz, float inv_nc, float ne_max, float* __restrict__ ws,
                                                      size_t ws_field)
 {
-    __shared__ float tile[32][33];
+    __shared__ float tile[32][129];
     const T* __restrict__ ne = static_cast<const T*>(fields.ne[blockIdx.z]);
     float* __restrict__ qt = ws + blockIdx.z * ws_field;
-    float* __restrict__ colsum = qt + (size_t)nz * padded_plane(nx, ny);
+    const size_t plane = padded_plane(nx, ny);
+    float* __restrict__ colsum = qt + (size_t)nz * plane;
+    const int nyp = padded_ny(ny);
     const int a = blockIdx.y;
     const int y0 = blockIdx.x * 32;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-    const int nyp = padded_ny(ny);
-    const size_t plane = padded_plane(nx, ny);
-    float acc = 0.f;  // column y0 + tx, summed by warp 0
-    for (int z0 = 0; z0 < nz; z0 += 32) {
-        for (int r = ty; r < 32; r += 8) {
-            const int y = y0 + r, z = z0 + tx;
-            float v = 0.f;
-            if (y < ny && z < nz) {
-                v = (float)ne[((size_t)a * ny + y) * nz + z] * inv_nc;
-                v = v < ne_max ? v : ne_max;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float part[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int z0 = 0; z0 < nz; z0 += 128) {
+        float v[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int y = y0 + w + 8 * i;
+            if (y < ny) {
+                load4<VEC>(ne + ((size_t)a * ny + y) * nz, z0 + 4 * lane, nz, v[i]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) v[i][j] = 0.f;
             }
-            tile[r][tx] = v;
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int z = z0 + 4 * lane + j;
+                float q = v[i][j] * inv_nc;
+                q = q < ne_max ? q : ne_max;
+                tile[w + 8 * i][4 * lane + j] = q;
+                part[i] = fmaf((z == 0 || z == nz - 1) ? 0.5f : (z < nz ? 1.f : 0.f), q, part[i]);
+            }
         }
         __syncthreads();
-        for (int r = ty; r < 32; r += 8) {
-            const int z = z0 + r, y = y0 + tx;
-            if (y < ny && z < nz) qt[(size_t)z * plane + (size_t)(a + 1) * nyp + y + kPadY] = tile[tx][r];
-        }
-        if (ty == 0) {
-            const int zend = min(32, nz - z0);
-            for (int r = 0; r < zend; ++r) {
-                const int z = z0 + r;
-                acc = fmaf((z == 0 || z == nz - 1) ? 0.5f : 1.f, tile[tx][r], acc);
-            }
+        const int y = y0 + lane;
+        for (int zz = w; zz < 128; zz += 8) {
+            const int z = z0 + zz;
+            if (z < nz && y < ny) qt[(size_t)z * plane + (size_t)(a + 1) * nyp + y + kPadY] = tile[lane][zz];
         }
         __syncthreads();
     }
-    if (ty == 0 && y0 + tx < ny) colsum[(size_t)a * ny + y0 + tx] = acc;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) part[i] += __shfl_xor_sync(0xffffffffu, part[i], off);
+        const int y = y0 + w + 8 * i;
+        if (lane == 0 && y < ny) colsum[(size_t)a * ny + y] = part[i];
+    }
 }
 
 // Ghost border of every plane: rows x = -1, nx (over y in [0, ny)) and columns
@@ -360,18 +403,26 @@ template <typename Stride>
 __device__ __forceinline__ PlaneSample sample_node(const float* c, const float* m, const float* p, Stride ry, float dz,
                                                    float fx, float fy)
 {
-    const float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w01 = (1.f - fx) * fy, w11 = fx * fy;
+    // corners as (value, d/dz) and (d/dx, d/dy) pairs; packed FP32x2 arithmetic
     const float q00 = c[0], q10 = c[ry], q01 = c[1], q11 = c[ry + 1];
-    const float gx00 = q10 - c[-ry], gx10 = c[2 * ry] - q00;
-    const float gx01 = q11 - c[1 - ry], gx11 = c[2 * ry + 1] - q01;
-    const float gy00 = q01 - c[-1], gy01 = c[2] - q00;
-    const float gy10 = q11 - c[ry - 1], gy11 = c[ry + 2] - q10;
-    const float gz = w00 * (p[0] - m[0]) + w10 * (p[ry] - m[ry]) + w01 * (p[1] - m[1]) + w11 * (p[ry + 1] - m[ry + 1]);
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 Z00 = __ffma2_rn(make_float2(m[0], m[ry]), m1, make_float2(p[0], p[ry]));
+    const float2 Z01 = __ffma2_rn(make_float2(m[1], m[ry + 1]), m1, make_float2(p[1], p[ry + 1]));
+    const float2 G00 = __ffma2_rn(make_float2(c[-ry], c[-1]), m1, make_float2(q10, q01));
+    const float2 G10 = __ffma2_rn(make_float2(q00, c[ry - 1]), m1, make_float2(c[2 * ry], q11));
+    const float2 G01 = __ffma2_rn(make_float2(c[1 - ry], q00), m1, make_float2(q11, c[2]));
+    const float2 G11 = __ffma2_rn(make_float2(q01, q10), m1, make_float2(c[2 * ry + 1], c[ry + 2]));
+    const float2 X = make_float2(fx, fx), Y = make_float2(fy, fy);
+    // bilinear as nested linear interpolation: along x at y = j and j + 1, then along y
+    auto lerp2 = [&](float2 a, float2 b, float2 t) { return __ffma2_rn(t, __ffma2_rn(a, m1, b), a); };
+    const float2 G = lerp2(lerp2(G00, G10, X), lerp2(G01, G11, X), Y);
+    const float2 Q = lerp2(lerp2(make_float2(q00, Z00.x), make_float2(q10, Z00.y), X),
+                           lerp2(make_float2(q01, Z01.x), make_float2(q11, Z01.y), X), Y);
     PlaneSample s;
-    s.q = w00 * q00 + w10 * q10 + w01 * q01 + w11 * q11;
-    s.gx = 0.5f * (w00 * gx00 + w10 * gx10 + w01 * gx01 + w11 * gx11);
-    s.gy = 0.5f * (w00 * gy00 + w10 * gy10 + w01 * gy01 + w11 * gy11);
-    s.gz = dz * gz;
+    s.q = Q.x;
+    s.gx = 0.5f * G.x;
+    s.gy = 0.5f * G.y;
+    s.gz = dz * Q.y;
     return s;
 }
 
@@ -398,7 +449,7 @@ struct MarchConsts {
 
 struct MarchRay {
     float u, v, tx, ty, ax, ay, e_prev, q0;
-    float phi, phi_c;  // Neumaier-compensated phase sum (per m)
+    float phi, phi_c;  // Kahan-compensated phase sum (per m)
 };
 
 __device__ __forceinline__ void march_accel(const PlaneSample& f, float sx, float sy, float q0, const MarchConsts& mc,
@@ -436,19 +487,18 @@ __device__ __forceinline__ void march_kick_drift(MarchRay& r, float h, const Mar
 }
 
 // Second half: the closing half kick with the fields s on the new plane (its
-// slope-dependent term from a predictor), and the trapezoid phase of the step.
+// slope-dependent term at the slope predicted with the previous step's
+// acceleration), and the trapezoid phase of the step.
 __device__ __forceinline__ void march_kick(MarchRay& r, float h, const PlaneSample& s, const MarchConsts& mc)
 {
     const float hh = 0.5f * h;
-    float bx, by;
-    march_accel(s, r.tx, r.ty, r.q0, mc, bx, by);
-    march_accel(s, fmaf(hh, bx, r.tx), fmaf(hh, by, r.ty), r.q0, mc, r.ax, r.ay);
+    march_accel(s, fmaf(hh, r.ax, r.tx), fmaf(hh, r.ay, r.ty), r.q0, mc, r.ax, r.ay);
     r.tx = fmaf(hh, r.ax, r.tx);
     r.ty = fmaf(hh, r.ay, r.ty);
     const float e = march_dphase(s, r.tx, r.ty);
-    const float d = hh * (r.e_prev + e);
-    const float t = r.phi + d;
-    r.phi_c += fabsf(r.phi) >= fabsf(d) ? (r.phi - t) + d : (d - t) + r.phi;
+    const float y = hh * (r.e_prev + e) - r.phi_c;
+    const float t = r.phi + y;
+    r.phi_c = (t - r.phi) - y;
     r.phi = t;
     r.e_prev = e;
 }
@@ -457,7 +507,7 @@ __device__ __forceinline__ void march_write(const MarchRay& r, double k0, int n,
 {
     out[p] = atanf(r.tx);
     out[n + p] = atanf(r.ty);
-    out[2 * n + p] = (float)(k0 * ((double)r.phi + (double)r.phi_c));
+    out[2 * n + p] = (float)(k0 * ((double)r.phi - (double)r.phi_c));
 }
 
 // Any pixel grid: one thread per ray, fields read from the padded q through L1/L2.
@@ -631,10 +681,20 @@ extern "C" int tt_march_maps_batched(const void* const* ne, int nfields, int ne_
     float* ws = static_cast<float*>(workspace);
     const size_t wsf = field_ws_floats(nx, ny, nz);
     const dim3 tg((ny + 31) / 32, nx, nfields);
-    if (ne_dtype == TT_F32)
-        plane_q_kernel<float><<<tg, 256, 0, s>>>(fields, nx, ny, nz, (float)(1.0 / nc), (float)ne_max, ws, wsf);
-    else
-        plane_q_kernel<double><<<tg, 256, 0, s>>>(fields, nx, ny, nz, (float)(1.0 / nc), (float)ne_max, ws, wsf);
+    bool vec = nz % 4 == 0;
+    for (int f = 0; f < nfields; ++f) vec = vec && (reinterpret_cast<uintptr_t>(ne[f]) & 15) == 0;
+    const float inv_nc = (float)(1.0 / nc), qmax = (float)ne_max;
+    if (ne_dtype == TT_F32) {
+        if (vec)
+            plane_q_kernel<float, true><<<tg, 256, 0, s>>>(fields, nx, ny, nz, inv_nc, qmax, ws, wsf);
+        else
+            plane_q_kernel<float, false><<<tg, 256, 0, s>>>(fields, nx, ny, nz, inv_nc, qmax, ws, wsf);
+    } else {
+        if (vec)
+            plane_q_kernel<double, true><<<tg, 256, 0, s>>>(fields, nx, ny, nz, inv_nc, qmax, ws, wsf);
+        else
+            plane_q_kernel<double, false><<<tg, 256, 0, s>>>(fields, nx, ny, nz, inv_nc, qmax, ws, wsf);
+    }
     TT_TRY(tt::launch_status("march_maps plane_q"));
     const long long nghost = (2LL * nx + 2LL * ny) * nz * nfields;
     plane_ghost_kernel<<<(unsigned)((nghost + 255) / 256), 256, 0, s>>>(nfields, nx, ny, nz, ws, wsf);
@@ -687,12 +747,18 @@ __device__ __forceinline__ float dmap(const float* __restrict__ f, int i, int j,
     return 0.5f * (r[j + 1] - r[j - 1]);
 }
 
-__global__ void shadow_kernel(const float* __restrict__ theta, int P, float inv_h, float D, float* __restrict__ I,
-                              float* __restrict__ div)
+// Map blockIdx.y of a batch: theta (2, P, P), I and div (P, P) per map; the
+// drift is D, or Dv[blockIdx.y] when Dv is given.
+__global__ void shadow_kernel(const float* __restrict__ theta, int P, float inv_h, float D, const double* __restrict__ Dv,
+                              float* __restrict__ I, float* __restrict__ div)
 {
     const int n = P * P;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
+    theta += (size_t)blockIdx.y * 2 * n;
+    if (I) I += (size_t)blockIdx.y * n;
+    if (div) div += (size_t)blockIdx.y * n;
+    if (Dv) D = (float)Dv[blockIdx.y];
     const int i = p / P, j = p % P;
     const float* tx = theta;
     const float* ty = theta + n;
@@ -715,6 +781,17 @@ extern "C" int tt_shadowgram(const float* theta, int P, double pitch, double D, 
     if (!intensity && !div) return TT_OK;
     const int n = P * P;
     shadow_kernel<<<(n + 255) / 256, 256, 0, tt::as_stream(stream)>>>(theta, P, (float)(1.0 / pitch), (float)D,
-                                                                       intensity, div);
+                                                                       nullptr, intensity, div);
     return tt::launch_status("shadowgram");
+}
+
+extern "C" int tt_shadowgram_batched(const float* theta, int nmaps, int P, double pitch, const double* D,
+                                     float* intensity, void* stream)
+{
+    if (!theta || !D || !intensity || nmaps < 1 || nmaps > 65535 || P < 2 || !(pitch > 0))
+        return tt::invalid("shadowgram_batched: bad arguments");
+    const int n = P * P;
+    shadow_kernel<<<dim3((n + 255) / 256, nmaps), 256, 0, tt::as_stream(stream)>>>(theta, P, (float)(1.0 / pitch),
+                                                                                    0.f, D, intensity, nullptr);
+    return tt::launch_status("shadowgram_batched");
 }

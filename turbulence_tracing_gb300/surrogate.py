@@ -119,14 +119,13 @@ def encode_batch(mm, S, out):
     """Network inputs out (n, 6, S, S) and the scales s (n,) from march outputs
     mm (n, 5, S, S): straight and marched deflections / s, the marched phase
     standardised per field, log10 of the straight-line drift in cells."""
-    s = torch.sqrt((mm[:, 3:5].double() ** 2).mean(dim=(1, 2, 3))).float().clamp_min(1e-30)
+    s = torch.sqrt((mm[:, 3:5] ** 2).mean(dim=(1, 2, 3))).clamp_min(1e-30)
     sb = s[:, None, None, None]
     out[:, 0:2] = mm[:, 3:5] / sb
     out[:, 2:4] = mm[:, 0:2] / sb
-    ph = mm[:, 2].double()
-    mu = ph.mean(dim=(1, 2), keepdim=True)
-    sd = ph.std(dim=(1, 2), keepdim=True).clamp_min(1e-30)
-    out[:, 4] = ((ph - mu) / sd).float()
+    ph = mm[:, 2]
+    sd, mu = torch.std_mean(ph, dim=(1, 2), keepdim=True)
+    out[:, 4] = (ph - mu) / sd.clamp_min(1e-30)
     out[:, 5] = torch.log10(s * (S - 1))[:, None, None]
     return s
 
@@ -297,54 +296,102 @@ def calibrate(res, quantile=0.9):
     return float(np.quantile(r, quantile))
 
 
-class Pipeline:
-    """Surrogate with fallback, a chunk of fields at a time: one batched march
-    over the chunk (marched and straight-line maps) -> network -> shadowgrams
-    and error estimates, all on the device with one host read per chunk (the
-    estimates); the fields whose estimate exceeds tol are traced exactly.  The
-    detector drift D of each field is part of its detector set-up (given)."""
+class _Slot:
+    """Buffers (and the captured graph) for one chunk in flight."""
 
-    def __init__(self, W, net, kappa, tol=0.02, batch=8):
-        self.W, self.net, self.kappa, self.tol, self.B = W, net, kappa, tol, batch
+    def __init__(self, W, batch):
         S, dev = W.S, W.dev
         self.X = torch.empty((batch, W.in_ch, S, S), dtype=torch.float32, device=dev)
         self.out = torch.empty((batch, 3, S, S), dtype=torch.float32, device=dev)
-        self.mar = torch.empty((batch, W.n_maps, S, S), dtype=torch.float32, device=dev)
+        self.mar = torch.zeros((batch, W.n_maps, S, S), dtype=torch.float32, device=dev)
         self.theta = torch.empty((batch, 2, S, S), dtype=torch.float32, device=dev)
-        self.I = torch.empty((batch, 2, S, S), dtype=torch.float32, device=dev)
-        self.ws = None
+        self.theta_m = torch.empty((batch, 2, S, S), dtype=torch.float32, device=dev)
+        self.I_n = torch.empty((batch, S, S), dtype=torch.float32, device=dev)
+        self.I_m = torch.empty((batch, S, S), dtype=torch.float32, device=dev)
+        self.D = torch.ones(batch, dtype=torch.float64, device=dev)
+        self.D_host = torch.ones(batch, dtype=torch.float64).pin_memory()
+        self.est = torch.empty(batch, dtype=torch.float32, device=dev)
+        self.est_host = torch.empty(batch, dtype=torch.float32).pin_memory()
+        self.ready = torch.cuda.Event()
+        self.graph = None
+
+
+class Pipeline:
+    """Surrogate with fallback, a chunk of fields at a time: one batched march
+    over the chunk (marched and straight-line maps), then one CUDA-graph replay
+    of the rest -- encoding, network, decoding, the two shadowgrams of every
+    field (network and march) and the error estimates -- whose estimates
+    come back to the host asynchronously while the next chunk already runs
+    (two chunks in flight); the fields whose estimate exceeds tol are traced
+    exactly.  The detector drift D of each field is part of its detector
+    set-up (given)."""
+
+    def __init__(self, W, net, kappa, tol=0.02, batch=8, graph=True):
+        self.W, self.net, self.kappa, self.tol, self.B = W, net, kappa, tol, batch
+        self.ws = torch.empty(core.march_batched_workspace_bytes(batch, (W.S, W.S, W.S)), dtype=torch.uint8,
+                              device=W.dev)
+        self.slots = [_Slot(W, batch), _Slot(W, batch)]
+        for sl in self.slots:
+            self._post(sl)
+            torch.cuda.synchronize()
+            if graph:
+                st = torch.cuda.Stream()
+                st.wait_stream(torch.cuda.current_stream())
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.stream(st):
+                    with torch.cuda.graph(g):
+                        self._post(sl)
+                torch.cuda.current_stream().wait_stream(st)
+                sl.graph = g
+
+    def _post(self, sl):
+        W = self.W
+        s = encode_batch(sl.mar, W.S, sl.X)
+        self.net.forward(sl.X, out=sl.out)
+        torch.addcmul(sl.mar[:, 0:2], s[:, None, None, None] / W.gain[None, 0:2, None, None], sl.out[:, 0:2],
+                      out=sl.theta)
+        sl.theta_m.copy_(sl.mar[:, 0:2])
+        core.shadowgram_batched(sl.theta, W.pitch, sl.D, intensity=sl.I_n)
+        core.shadowgram_batched(sl.theta_m, W.pitch, sl.D, intensity=sl.I_m)
+        torch.mul(torch.linalg.norm(sl.I_n - sl.I_m, dim=(1, 2)) / torch.linalg.norm(sl.I_n, dim=(1, 2)),
+                  self.kappa, out=sl.est)
+
+    def _launch(self, sl, chunk, D):
+        W, n = self.W, len(chunk)
+        sl.D_host[:n] = torch.as_tensor(D, dtype=torch.float64)
+        sl.D.copy_(sl.D_host, non_blocking=True)
+        core.march_maps_batched(chunk, W.x, W.x, W.x, W.S, lwl=W.lwl, out=sl.mar[:n], ws=self.ws)
+        if sl.graph is not None:
+            sl.graph.replay()
+        else:
+            self._post(sl)
+        sl.est_host.copy_(sl.est, non_blocking=True)
+        sl.ready.record()
 
     def run(self, fields, Ds):
         """fields: list of density tensors, Ds: their drifts.  Returns
         (intensity list, fell_back list)."""
-        W, S = self.W, self.W.S
+        W = self.W
+        chunks = [(fields[b:b + self.B], Ds[b:b + self.B]) for b in range(0, len(fields), self.B)]
         I_out, fell = [], []
-        for b0 in range(0, len(fields), self.B):
-            chunk, D = fields[b0:b0 + self.B], Ds[b0:b0 + self.B]
+        if not chunks:
+            return I_out, fell
+        self._launch(self.slots[0], *chunks[0])
+        for c, (chunk, D) in enumerate(chunks):
+            sl = self.slots[c % 2]
             n = len(chunk)
-            if self.ws is None:
-                need = core.march_batched_workspace_bytes(self.B, chunk[0].shape)
-                self.ws = torch.empty(need, dtype=torch.uint8, device=W.dev)
-            core.march_maps_batched(chunk, W.x, W.x, W.x, S, lwl=W.lwl, out=self.mar[:n], ws=self.ws)
-            s = encode_batch(self.mar[:n], S, self.X[:n])
-            if n == self.B:
-                self.net.forward(self.X, out=self.out)
-            else:
-                self.out[:n] = self.net.forward(self.X[:n].contiguous())
-            self.theta[:n] = self.mar[:n, 0:2] + (s[:, None, None, None] / W.gain[None, 0:2, None, None]) * \
-                self.out[:n, 0:2]
-            for i in range(n):
-                W.shadow(self.theta[i], D[i], out=self.I[i, 0])
-                W.shadow(self.mar[i, 0:2], D[i], out=self.I[i, 1])
-            In, Im = self.I[:n, 0].double(), self.I[:n, 1].double()
-            est = (self.kappa * torch.linalg.norm(In - Im, dim=(1, 2)) / torch.linalg.norm(In, dim=(1, 2))).tolist()
+            keep = [sl.I_n[i].clone() for i in range(n)]  # before the slot is reused
+            if c + 1 < len(chunks):
+                self._launch(self.slots[(c + 1) % 2], *chunks[c + 1])
+            sl.ready.synchronize()
+            est = sl.est_host[:n].tolist()
             for i in range(n):
                 if est[i] > self.tol:
                     theta, _, _ = W.trace(chunk[i])
                     I_out.append(W.shadow(theta, D[i]))
                     fell.append(True)
                 else:
-                    I_out.append(self.I[i, 0].clone())
+                    I_out.append(keep[i])
                     fell.append(False)
         return I_out, fell
 

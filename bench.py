@@ -75,6 +75,7 @@ def parse():
     ap.add_argument("--sur-train", type=int, default=2048)
     ap.add_argument("--sur-test", type=int, default=96)
     ap.add_argument("--sur-epochs", type=int, default=15)
+    ap.add_argument("--sur-batch", type=int, default=16, help="fields per chunk in the surrogate pipeline")
     ap.add_argument("--json-out", default="")
     return ap.parse_args()
 
@@ -506,11 +507,11 @@ def surrogate_run(a):
     fields = [W.field(p) for p in params]
     # detector set-up: each field's drift for 20% straight-line contrast
     Ds = [float(W.drift(W.maps(f))) for f in fields]
-    pipe = SG.Pipeline(W, net, kappa)
-    bt = SG.BatchedTracer(W)
-    pipe.run(fields[:8], Ds[:8])
+    pipe = SG.Pipeline(W, net, kappa, batch=a.sur_batch)
+    bt = SG.BatchedTracer(W, batch=a.sur_batch)
+    pipe.run(fields[:a.sur_batch], Ds[:a.sur_batch])
     pipe.run_tracer(fields[:2], Ds[:2])
-    bt.run(fields[:8], Ds[:8])
+    bt.run(fields[:a.sur_batch], Ds[:a.sur_batch])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     I_p, fell = pipe.run(fields, Ds)
@@ -547,7 +548,7 @@ def surrogate_run(a):
                                "unit": "GB/s", "frac": march_bytes / (us_march_b * 1e-6) / 1e9 / peak,
                                "launch": "8 fields per launch",
                                "bytes_per_field": march_bytes, "peak_kind": peak_kind},
-            "pipeline": {"kappa": kappa, "tol": 0.02, "fallback_fraction": float(np.mean(fell)),
+            "pipeline": {"kappa": kappa, "tol": 0.02, "chunk": a.sur_batch, "fallback_fraction": float(np.mean(fell)),
                          "err_max": max(errs), "accepted_err_max": max(acc) if acc else None,
                          "accepted_err_mean": float(np.mean(acc)) if acc else None,
                          "pipeline_s": t_pipe, "tracer_per_field_s": t_tr, "tracer_batched_s": t_bt,

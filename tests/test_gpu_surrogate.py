@@ -238,3 +238,16 @@ def test_trained_surrogate_gains_and_fallback_bounds_error(cuda):
     acc = est <= 0.02
     assert acc.mean() >= 0.5
     assert np.all(e_n[24:][acc] <= 0.02), e_n[24:][acc]
+
+    # the pipeline (batched march, graph-captured network and estimates, two
+    # chunks in flight, a partial last chunk) against tracing every field, one
+    # field per launch and a chunk per batched launch
+    fields = [W.field(p) for p in SG.draw_fields(12, seed=3)]
+    Ds = [float(W.drift(W.maps(f))) for f in fields]
+    I_p, fell = SG.Pipeline(W, net, kappa, batch=8).run(fields, Ds)
+    I_t = SG.Pipeline(W, net, kappa, batch=8, graph=False).run_tracer(fields, Ds)
+    I_b = SG.BatchedTracer(W, batch=8).run(fields, Ds)
+    assert len(I_p) == len(fell) == 12
+    for p_, t_, b_, f_ in zip(I_p, I_t, I_b, fell):
+        assert torch.equal(b_, t_)
+        assert SG.rel_l2(p_, t_) <= (1e-6 if f_ else 0.02)

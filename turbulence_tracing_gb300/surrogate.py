@@ -436,3 +436,45 @@ class BatchedTracer:
                 theta = torch.stack([rf[1].view(S, S), rf[3].view(S, S)]).float()
                 res.append(W.shadow(theta, D[i]))
         return res
+
+
+def _main(argv=None):
+    """Time the batched march and the network forward on seeded fields:
+    python -m turbulence_tracing_gb300.surrogate --size 256 --fields 8 --reps 3"""
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--fields", type=int, default=8)
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args(argv)
+    W = Workload(a.size)
+    fields = [W.field(p) for p in draw_fields(a.fields, seed=14)]
+    out = torch.empty((a.fields, N_MAPS, a.size, a.size), dtype=torch.float32, device=W.dev)
+    ws = torch.empty(core.march_batched_workspace_bytes(a.fields, fields[0].shape), dtype=torch.uint8, device=W.dev)
+    net = fno_mod.FNO(a.size, in_ch=IN_CHANNELS, out_ch=3, layers=4, seed=0)
+    X = torch.empty((a.fields, IN_CHANNELS, a.size, a.size), dtype=torch.float32, device=W.dev)
+    y = None
+
+    def one():
+        nonlocal y
+        core.march_maps_batched(fields, W.x, W.x, W.x, a.size, lwl=W.lwl, out=out, ws=ws)
+        encode_batch(out, a.size, X)
+        y = net.forward(X, out=y)
+
+    one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.reps):
+        one()
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"size": a.size, "fields": a.fields,
+                      "march_and_forward_us_per_field": e0.elapsed_time(e1) * 1e3 / (a.reps * a.fields),
+                      "error_flag": net.error_flag()}))
+
+
+if __name__ == "__main__":
+    _main()

@@ -76,6 +76,9 @@ def parse():
     ap.add_argument("--sur-test", type=int, default=96)
     ap.add_argument("--sur-epochs", type=int, default=15)
     ap.add_argument("--sur-batch", type=int, default=16, help="fields per chunk in the surrogate pipeline")
+    ap.add_argument("--no-screen", action="store_true", help="skip the per-tile screening of the stress field")
+    ap.add_argument("--screen-n", type=int, default=1024, help="stress-field grid for the tile screening leg")
+    ap.add_argument("--screen-train", type=int, default=8, help="training fields (16 tiles each at 1024^3)")
     ap.add_argument("--json-out", default="")
     return ap.parse_args()
 
@@ -307,6 +310,9 @@ def run_ours(a):
     if rank == 0 and not a.no_surrogate:
         torch.cuda.empty_cache()
         res["surrogate"] = surrogate_run(a)
+    if rank == 0 and not a.no_screen:
+        torch.cuda.empty_cache()
+        res["screen"] = screen_run(a)
     if rank == 0 and not a.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(a, ne, x)
     if dist:
@@ -556,6 +562,60 @@ def surrogate_run(a):
                          "speedup_vs_tracer_per_field": t_tr / t_pipe,
                          "speedup_vs_tracer_batched": t_bt / t_pipe},
             "error_flag": net.error_flag()}
+
+
+def screen_run(a):
+    """The stress field's surrogate screening (1024^3, L = 10 mm, -11/3,
+    delta = 0.3, 1e25 m^-3): the network, trained on 256^2 tiles of other
+    realisations of the same configuration, screens the field per tile and
+    only flagged tiles are re-traced; timed against tracing all N^2 pixel-centre
+    rays (volume build + trace), both followed by the field's shadowgram."""
+    import time
+
+    import torch
+
+    from turbulence_tracing_gb300 import fno, surrogate as SG
+
+    N = a.screen_n
+    W = SG.Workload(N, L=10e-3 * N / 1024)
+
+    def stress(seed):
+        return dict(alpha=-11.0 / 3.0, delta=0.3, ne0=1e25, seed=seed)
+
+    t0 = time.perf_counter()
+    X, Y, _, _ = SG.build_tile_dataset(W, [stress(a.seed + 500 + i) for i in range(a.screen_train)])
+    Xc, _, sc, tc = SG.build_tile_dataset(W, [stress(a.seed + 600), stress(a.seed + 601)], keep_truth=True)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    net = fno.FNO(SG.TILE, in_ch=W.in_ch, out_ch=3, layers=4, seed=a.seed)
+    hist, _ = SG.Trainer(net, X, Y, batch=8).fit(8, lr=1e-3)
+    fields = [W.field(stress(a.seed + 700 + i)) for i in range(2)]
+    Ds = [float(W.drift(W.march(f)[3:5])) for f in fields]
+    tiles = SG.tile_errors(W, net, Xc, sc, tc, Ds[0])
+    kappa = SG.calibrate(tiles)
+    scr = SG.TileScreen(W, net, kappa)
+    scr.run(fields[0], Ds[0])
+    W.trace(fields[0])
+    out = []
+    for f, D in zip(fields, Ds):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        I_s, _, flagged = scr.run(f, D)
+        torch.cuda.synchronize()
+        t_scr = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        th, _, steps = W.trace(f)
+        I_t = W.shadow(th, D)
+        torch.cuda.synchronize()
+        t_tr = time.perf_counter() - t0
+        out.append({"screen_s": t_scr, "tracer_s": t_tr, "speedup": t_tr / t_scr, "flagged_tiles": len(flagged),
+                    "tiles": scr.nt, "shadow_err": SG.rel_l2(I_s, I_t), "tracer_ray_steps": int(steps)})
+    return {"grid": N, "tile": SG.TILE, "train_fields": a.screen_train, "train_tiles": int(X.shape[0]),
+            "data_s": t_data, "loss_first_last": [hist[0], hist[-1]], "kappa": kappa,
+            "calibration_tiles": {"err_march_mean": float(np.mean([r["err_march"] for r in tiles])),
+                                  "err_net_mean": float(np.mean([r["err_net"] for r in tiles])),
+                                  "err_straight_mean": float(np.mean([r["err_straight"] for r in tiles]))},
+            "fields": out, "error_flag": net.error_flag()}
 
 
 def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):

@@ -251,3 +251,32 @@ def test_trained_surrogate_gains_and_fallback_bounds_error(cuda):
     for p_, t_, b_, f_ in zip(I_p, I_t, I_b, fell):
         assert torch.equal(b_, t_)
         assert SG.rel_l2(p_, t_) <= (1e-6 if f_ else 0.02)
+
+
+def test_tile_screening_of_a_large_field(cuda):
+    """The stress form at 512^3: the network screens the field per 256^2 tile
+    and only flagged tiles are re-traced; the assembled shadowgram is within
+    2% of the exact trace, and a screen that flags every tile reproduces the
+    exact trace's deflection bit for bit."""
+    from turbulence_tracing_gb300 import fno, surrogate as SG
+
+    W = SG.Workload(512, L=5e-3)
+
+    def stress(seed):
+        return dict(alpha=-11.0 / 3.0, delta=0.3, ne0=1e25, seed=seed)
+
+    X, Y, _, _ = SG.build_tile_dataset(W, [stress(100 + i) for i in range(6)])
+    net = fno.FNO(256, in_ch=W.in_ch, out_ch=3, layers=4, seed=0)
+    SG.Trainer(net, X, Y, batch=8).fit(4, lr=1e-3)
+    Xc, _, sc, tc = SG.build_tile_dataset(W, [stress(200), stress(201)], keep_truth=True)
+    ne = W.field(stress(300))
+    D = float(W.drift(W.march(ne)[3:5]))
+    kappa = SG.calibrate(SG.tile_errors(W, net, Xc, sc, tc, D))
+    I, theta, flagged = SG.TileScreen(W, net, kappa).run(ne, D)
+    assert net.error_flag() == 0
+    th_t, _, _ = W.trace(ne)
+    I_t = W.shadow(th_t, D)
+    assert SG.rel_l2(I, I_t) <= 0.02, (SG.rel_l2(I, I_t), flagged)
+    _, theta_all, flagged_all = SG.TileScreen(W, net, kappa, tol=-1.0).run(ne, D)
+    assert flagged_all == [0, 1, 2, 3]
+    assert torch.equal(theta_all, th_t)

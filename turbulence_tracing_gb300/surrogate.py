@@ -438,6 +438,133 @@ class BatchedTracer:
         return res
 
 
+
+# ---------------------------------------------------------------------------
+# Screening a large field per 256^2 tile
+# ---------------------------------------------------------------------------
+TILE = 256
+
+
+def tile_maps(m, T=TILE):
+    """(C, N, N) -> (n_tiles, C, T, T), tiles in row-major order, contiguous."""
+    C, N, _ = m.shape
+    k = N // T
+    return m.reshape(C, k, T, k, T).permute(1, 3, 0, 2, 4).reshape(k * k, C, T, T).contiguous()
+
+
+def untile(t, N):
+    """(n_tiles, C, T, T) -> (C, N, N), the inverse of tile_maps."""
+    _, C, T, _ = t.shape
+    k = N // T
+    return t.reshape(k, k, C, T, T).permute(2, 0, 3, 1, 4).reshape(C, N, N)
+
+
+def tile_pixels(N, t, T=TILE, device=None):
+    """Flat pixel indices (pi * N + pj) of tile t, row-major within the tile."""
+    k = N // T
+    ti, tj = divmod(t, k)
+    r = torch.arange(T, device=device)
+    return ((ti * T + r)[:, None] * N + (tj * T + r)[None, :]).reshape(-1)
+
+
+def build_tile_dataset(W, params, keep_truth=False):
+    """Network inputs and targets for the 256^2 tiles of W.S^3 fields (W.S a
+    multiple of 256): one march and one exact trace per field, cut into tiles;
+    per-tile scales.  Returns X, Y, scales, truth (tile maps and exact tile
+    deflections/phases, optional)."""
+    N, T = W.S, TILE
+    if N % T:
+        raise ValueError("field size must be a multiple of %d" % T)
+    nt = (N // T) ** 2
+    M = len(params) * nt
+    X = torch.empty((M, IN_CHANNELS, T, T), dtype=torch.float32, device=W.dev)
+    Y = torch.empty((M, 3, T, T), dtype=torch.float32, device=W.dev)
+    scale = torch.empty(M, dtype=torch.float32, device=W.dev)
+    truth = None
+    if keep_truth:
+        truth = {"march": torch.empty((M, N_MAPS, T, T), dtype=torch.float32, device=W.dev),
+                 "theta": torch.empty((M, 2, T, T), dtype=torch.float32, device=W.dev),
+                 "phase": torch.empty((M, T, T), dtype=torch.float64, device=W.dev)}
+    for f, p in enumerate(params):
+        ne = W.field(p)
+        mt = tile_maps(W.march(ne))
+        theta, phase, _ = W.trace(ne)
+        tt, pt = tile_maps(theta), tile_maps(phase[None])
+        sl = slice(f * nt, (f + 1) * nt)
+        scale[sl] = encode_batch(mt, T, X[sl])
+        for t in range(nt):
+            Y[f * nt + t] = targets(mt[t], tt[t], pt[t, 0], scale[f * nt + t], W.k0, W.L)
+        if keep_truth:
+            truth["march"][sl], truth["theta"][sl], truth["phase"][sl] = mt, tt, pt[:, 0]
+    if W.gain is None:
+        W.gain = (1.0 / torch.sqrt((Y.double() ** 2).mean(dim=(0, 2, 3))).clamp_min(1e-30)).float()
+    Y *= W.gain[None, :, None, None]
+    return X, Y, scale, truth
+
+
+def tile_errors(W, net, X, scale, truth, D, batch=16):
+    """Per-tile shadowgram errors (tile-local shadowgrams at drift D) of the march
+    and the network, and the network's correction size."""
+    out = predict(net, X, batch)
+    res = []
+    for i in range(X.shape[0]):
+        mm = truth["march"][i]
+        th_net, _ = decode(out[i], mm, scale[i], W.k0, W.L, W.gain)
+        I_t = W.shadow(truth["theta"][i], D)
+        I_m = W.shadow(mm[0:2], D)
+        I_n = W.shadow(th_net, D)
+        res.append({"err_march": rel_l2(I_m, I_t), "err_net": rel_l2(I_n, I_t),
+                    "err_straight": rel_l2(W.shadow(mm[3:5], D), I_t),
+                    "moved": rel_l2(I_n, I_m) * float(torch.linalg.norm(I_m.double()) / torch.linalg.norm(I_n.double()))})
+    return res
+
+
+class TileScreen:
+    """Surrogate screening of one N^3 field per 256^2 tile: one march over the
+    whole field at N^2 pixel rays, the network on all tiles as one batch, a
+    per-tile error estimate (kappa x how far the network moved the tile's
+    shadowgram from the march's), and an exact FP32 trace of the pixel rays of
+    the flagged tiles only; the tiles are assembled into the field's
+    deflection map and shadowgram."""
+
+    def __init__(self, W, net, kappa, tol=0.02):
+        if W.S % TILE:
+            raise ValueError("field size must be a multiple of %d" % TILE)
+        self.W, self.net, self.kappa, self.tol = W, net, kappa, tol
+        self.nt = (W.S // TILE) ** 2
+        self.X = torch.empty((self.nt, IN_CHANNELS, TILE, TILE), dtype=torch.float32, device=W.dev)
+        self.out = torch.empty((self.nt, 3, TILE, TILE), dtype=torch.float32, device=W.dev)
+        self.vol = None
+        self.trace_out = None
+
+    def run(self, ne, D):
+        """Returns (intensity (N, N), deflection (2, N, N), flagged tile indices)."""
+        W, N, T = self.W, self.W.S, TILE
+        mt = tile_maps(W.march(ne))
+        s = encode_batch(mt, T, self.X)
+        self.net.forward(self.X, out=self.out)
+        th = torch.addcmul(mt[:, 0:2], s[:, None, None, None] / W.gain[None, 0:2, None, None], self.out[:, 0:2])
+        Dv = torch.full((self.nt,), float(D), dtype=torch.float64, device=W.dev)
+        I_n = core.shadowgram_batched(th, W.pitch, Dv)
+        I_m = core.shadowgram_batched(mt[:, 0:2].contiguous(), W.pitch, Dv)
+        est = (self.kappa * torch.linalg.norm((I_n - I_m).double(), dim=(1, 2)) /
+               torch.linalg.norm(I_n.double(), dim=(1, 2))).tolist()
+        flagged = [t for t in range(self.nt) if est[t] > self.tol]
+        theta = untile(th, N).contiguous()
+        if flagged:
+            self.vol = core.build_volume(ne, W.x, W.x, W.x, 2, lwl=W.lwl,
+                                         nodes=None if self.vol is None else self.vol.nodes)
+            idx = torch.cat([tile_pixels(N, t, device=W.dev) for t in flagged])
+            # phase on, as Workload.trace: the phase takes part in step control, and on
+            # a field with caustics a different step sequence moves rays measurably
+            o = core.trace_f32(self.vol, W.s0[:, idx].contiguous(), W.t_end, W.ext, rtol=W.rtol, phase=True,
+                               want_sf=False)
+            flat = theta.view(2, -1)
+            flat[0, idx] = o["rf"][1].float()
+            flat[1, idx] = o["rf"][3].float()
+        return W.shadow(theta, D), theta, flagged
+
+
 def _main(argv=None):
     """Time the batched march and the network forward on seeded fields:
     python -m turbulence_tracing_gb300.surrogate --size 256 --fields 8 --reps 3"""

@@ -1,7 +1,7 @@
 """K2 (solve/dsdt/dndr/ray_at_exit, particle_tracker.py:243-380, 398-419) on
 the GPU vs the oracle.
 
-Bars (the benchmark spec): positions within 1e-6 of the box length, angles within
+Bars: positions within 1e-6 of the box length, angles within
 1 urad, phase within 1e-3 rad of the FP64 oracle at rtol 1e-10."""
 import numpy as np
 import pytest

@@ -1,5 +1,5 @@
 """The learned surrogate end to end at 128^2: straight-line maps against a
-direct restatement, the exact tracer as the judge of held-out fields, and
+direct restatement, the exact tracer as the reference for held-out fields, and
 what the trained network gains over the straight-line method without it."""
 import numpy as np
 import pytest

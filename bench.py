@@ -157,6 +157,21 @@ def dist_setup():
     return ws, rank, local
 
 
+def across_ranks(units, seconds, dist, dev):
+    """Whole-job units and time over the replicas (one rank per GPU, each on
+    its own inputs): units summed, seconds maximised over ranks.  Without a
+    process group the local values are returned."""
+    if not dist:
+        return units, seconds
+    import torch
+
+    u = torch.tensor([float(units)], dtype=torch.float64, device=dev)
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=dev)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(u.item()), float(t.item())
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -269,12 +284,10 @@ def run_ours(a):
     ms_total = ev0.elapsed_time(ev1)
     trace_ms = [e0.elapsed_time(e1) for e0, e1 in tr_ev]
     ms_step = ms_total / a.steps
-    if dist:
-        t = torch.tensor([ms_step], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = ray_steps_step * ws / (ms_step / 1e3)
-    rays_per_s = Np * ws / (ms_step / 1e3)
+    steps_all, sec_step = across_ranks(ray_steps_step, ms_step / 1e3, dist, dev)
+    ms_step = sec_step * 1e3
+    value = steps_all / sec_step
+    rays_per_s = Np * ws / sec_step
 
     peak, peak_kind = peaks()
     trace_ms_avg = float(np.mean(trace_ms))
@@ -663,14 +676,11 @@ def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
         tot += rs
     torch.cuda.synchronize()
     sec = (time.perf_counter() - t0) / k
-    if dist:
-        t = torch.tensor([sec], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        sec = float(t.item())
+    units, sec = across_ranks(tot / k, sec, dist, dev)
     Np = s0_host.shape[1]
     h2d = Np * 6 * 8 + 3 * Np * 4 * 8 + Np * 8          # s0; rf re-uploaded by each diagnostic; phase weights
     d2h = Np * (6 + 4 + 1) * 8 + Np * 2 * 4 + 4 * det * det * 8  # sf, rf, phase; status, steps; 3 H + 1 Hw
-    return {"value": (tot / k) * ws / sec, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+    return {"value": units / sec, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "seconds_per_step": sec, "steps": k,
             "path": "ElectronCube.solve(precision='fp32', phase=True) + Shadowgraphy, Schlieren_KE, "
                     "phase-weighted Shadowgraphy histograms (numpy in, numpy out)"}

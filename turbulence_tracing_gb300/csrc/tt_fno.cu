@@ -473,57 +473,107 @@ __global__ void __launch_bounds__(128) fno_wgrad_kernel(int B, const bf16* __res
 
 // ----------------------------------------------------------------------------- y DFTs (FP32)
 // Y[b, m, c] = sum_y X[b, c, y, kx] exp(-2 pi i ky y / S) over the 32 retained ky.
+// One block per (b, c): kYdftSplit groups of 128 threads each sum a quarter of
+// the rows y for a 2 (ky) x 2 (kx) tile of modes per thread (4 shared loads
+// for 16 FMAs a row); the partial sums are added in shared memory in a fixed
+// order.
+constexpr int kYdftTile = 128;
+constexpr int kYdftSplit = 4;
+constexpr int kYdftThreads = kYdftTile * kYdftSplit;
+
 template <int S>
-__global__ void __launch_bounds__(256) fno_ydft_kernel(const float* __restrict__ X, const float2* __restrict__ tw,
-                                                       float2* __restrict__ Y)
+__global__ void __launch_bounds__(kYdftThreads) fno_ydft_kernel(const float* __restrict__ X,
+                                                                const float2* __restrict__ tw, float2* __restrict__ Y)
 {
-    __shared__ float xs[S * NJ];
+    static_assert(kYdftTile == (MD / 2) * (NJ / 2), "one 2 x 2 tile of modes per thread of a group");
+    static_assert(S % kYdftSplit == 0, "whole row quarters");
+    __shared__ __align__(16) float xs[S * NJ];
     __shared__ float2 tws[S];
+    __shared__ float4 part[kYdftSplit - 1][kYdftTile][2];
     const int bc = blockIdx.x, b = bc / W, c = bc % W;
     const float4* src = reinterpret_cast<const float4*>(X + (size_t)bc * S * NJ);
-    for (int i = threadIdx.x; i < S * NJ / 4; i += 256) reinterpret_cast<float4*>(xs)[i] = __ldg(src + i);
-    for (int i = threadIdx.x; i < S; i += 256) tws[i] = tw[i];
+    for (int i = threadIdx.x; i < S * NJ / 4; i += kYdftThreads) reinterpret_cast<float4*>(xs)[i] = __ldg(src + i);
+    for (int i = threadIdx.x; i < S; i += kYdftThreads) tws[i] = tw[i];
     __syncthreads();
-    for (int m = threadIdx.x; m < NM; m += 256) {
-        const int kyi = m / MD, kx = m % MD;
-        const int ky = kyi < MD ? kyi : S - NJ + kyi;
-        float ar = 0.f, ai = 0.f;
-#pragma unroll 8
-        for (int y = 0; y < S; ++y) {
-            const float2 e = tws[(ky * y) & (S - 1)];
-            const float xr = xs[y * NJ + kx], xi = xs[y * NJ + MD + kx];
-            ar = fmaf(xr, e.x, fmaf(xi, e.y, ar));
-            ai = fmaf(xi, e.x, fmaf(-xr, e.y, ai));
+    const int t = threadIdx.x % kYdftTile, g = threadIdx.x / kYdftTile;
+    const int kx0 = 2 * (t % (MD / 2)), kyi0 = 2 * (t / (MD / 2));
+    int ky[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) ky[q] = kyi0 + q < MD ? kyi0 + q : S - NJ + kyi0 + q;
+    float ar[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, ai[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    constexpr int RY = S / kYdftSplit;
+#pragma unroll 4
+    for (int y = g * RY; y < (g + 1) * RY; ++y) {
+        const float2 xr = *reinterpret_cast<const float2*>(xs + y * NJ + kx0);
+        const float2 xi = *reinterpret_cast<const float2*>(xs + y * NJ + MD + kx0);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const float2 e = tws[(ky[q] * y) & (S - 1)];
+            ar[q][0] = fmaf(xr.x, e.x, fmaf(xi.x, e.y, ar[q][0]));
+            ai[q][0] = fmaf(xi.x, e.x, fmaf(-xr.x, e.y, ai[q][0]));
+            ar[q][1] = fmaf(xr.y, e.x, fmaf(xi.y, e.y, ar[q][1]));
+            ai[q][1] = fmaf(xi.y, e.x, fmaf(-xr.y, e.y, ai[q][1]));
         }
-        Y[((size_t)b * NM + m) * W + c] = make_float2(ar, ai);
+    }
+    if (g > 0) {
+        part[g - 1][t][0] = make_float4(ar[0][0], ai[0][0], ar[0][1], ai[0][1]);
+        part[g - 1][t][1] = make_float4(ar[1][0], ai[1][0], ar[1][1], ai[1][1]);
+    }
+    __syncthreads();
+    if (g == 0) {
+#pragma unroll
+        for (int h = 0; h < kYdftSplit - 1; ++h) {
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const float4 v = part[h][t][q];
+                ar[q][0] += v.x, ai[q][0] += v.y, ar[q][1] += v.z, ai[q][1] += v.w;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+                Y[((size_t)b * NM + (kyi0 + q) * MD + kx0 + j) * W + c] = make_float2(ar[q][j], ai[q][j]);
     }
 }
 
 // X[b, c, y, kx] = sum_ky Y[b, m(ky, kx), c] exp(+2 pi i ky y / S).
+// One block per (b, c) of 2 S threads; a thread owns a kx pair and 4 rows y
+// (a 4 x 2 tile: 6 shared loads for 32 FMAs a ky).
 template <int S>
-__global__ void __launch_bounds__(256) fno_iydft_kernel(const float2* __restrict__ Y, const float2* __restrict__ tw,
-                                                        float* __restrict__ X)
+__global__ void __launch_bounds__(2 * S) fno_iydft_kernel(const float2* __restrict__ Y, const float2* __restrict__ tw,
+                                                          float* __restrict__ X)
 {
-    __shared__ float2 ys[NM];
+    constexpr int KXP = MD / 2;      // kx pairs
+    constexpr int YG = 2 * S / KXP;  // row groups: rows yg + YG r, r = 0..3
+    static_assert(4 * YG == S, "4 rows a thread");
+    __shared__ __align__(16) float2 ys[NM];
     __shared__ float2 tws[S];
     const int bc = blockIdx.x, b = bc / W, c = bc % W;
-    for (int m = threadIdx.x; m < NM; m += 256) ys[m] = Y[((size_t)b * NM + m) * W + c];
-    for (int i = threadIdx.x; i < S; i += 256) tws[i] = tw[i];
+    for (int m = threadIdx.x; m < NM; m += 2 * S) ys[m] = Y[((size_t)b * NM + m) * W + c];
+    for (int i = threadIdx.x; i < S; i += 2 * S) tws[i] = tw[i];
     __syncthreads();
     float* dst = X + (size_t)bc * S * NJ;
-    for (int it = threadIdx.x; it < S * MD; it += 256) {
-        const int y = it / MD, kx = it % MD;
-        float xr = 0.f, xi = 0.f;
-#pragma unroll 8
-        for (int kyi = 0; kyi < NJ; ++kyi) {
-            const int ky = kyi < MD ? kyi : S - NJ + kyi;
-            const float2 e = tws[(ky * y) & (S - 1)];
-            const float2 u = ys[kyi * MD + kx];
-            xr = fmaf(u.x, e.x, fmaf(-u.y, e.y, xr));
-            xi = fmaf(u.x, e.y, fmaf(u.y, e.x, xi));
+    const int kx0 = 2 * (threadIdx.x % KXP), yg = threadIdx.x / KXP;
+    float xr[4][2] = {}, xi[4][2] = {};
+#pragma unroll 4
+    for (int kyi = 0; kyi < NJ; ++kyi) {
+        const int ky = kyi < MD ? kyi : S - NJ + kyi;
+        const float4 u = *reinterpret_cast<const float4*>(ys + kyi * MD + kx0);  // (u0.x, u0.y, u1.x, u1.y)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const float2 e = tws[(ky * (yg + r * YG)) & (S - 1)];
+            xr[r][0] = fmaf(u.x, e.x, fmaf(-u.y, e.y, xr[r][0]));
+            xi[r][0] = fmaf(u.x, e.y, fmaf(u.y, e.x, xi[r][0]));
+            xr[r][1] = fmaf(u.z, e.x, fmaf(-u.w, e.y, xr[r][1]));
+            xi[r][1] = fmaf(u.z, e.y, fmaf(u.w, e.x, xi[r][1]));
         }
-        dst[y * NJ + kx] = xr;
-        dst[y * NJ + MD + kx] = xi;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int y = yg + r * YG;
+        *reinterpret_cast<float2*>(dst + y * NJ + kx0) = make_float2(xr[r][0], xr[r][1]);
+        *reinterpret_cast<float2*>(dst + y * NJ + MD + kx0) = make_float2(xi[r][0], xi[r][1]);
     }
 }
 
@@ -960,11 +1010,11 @@ int forward_layers(const tt_fno_dims& d, const ParamLayout& P, const float* para
     for (int l = 0; l < d.layers; ++l) {
         float2* T2 = at<float2>(ws, L.t2) + (training ? (size_t)l * B * NM * W : 0);
         TT_TRY(launch_rowdft<S>(v(l), (long long)B * W * S, at<void>(ws, L.fxt), row, err, st));
-        fno_ydft_kernel<S><<<B * W, 256, 0, st>>>(row, tw, T2);
+        fno_ydft_kernel<S><<<B * W, kYdftThreads, 0, st>>>(row, tw, T2);
         TT_TRY(tt::launch_status("fno_ydft_kernel"));
         fno_specmix_fwd_kernel<<<NM, 256, 0, st>>>(B, reinterpret_cast<const float2*>(params + P.Rl[l]), T2, U);
         TT_TRY(tt::launch_status("fno_specmix_fwd_kernel"));
-        fno_iydft_kernel<S><<<B * W, 256, 0, st>>>(U, tw, row);
+        fno_iydft_kernel<S><<<B * W, 2 * S, 0, st>>>(U, tw, row);
         TT_TRY(tt::launch_status("fno_iydft_kernel"));
         bf16* z = training ? at<bf16>(ws, L.z + L.act * (size_t)l) : nullptr;
         TT_TRY((launch_mix<S, 0>(B, v(l), at<bf16>(ws, L.wpack) + (size_t)l * 2 * W * W, at<void>(ws, L.gt), row,
@@ -1019,12 +1069,12 @@ int run_train(const tt_fno_dims& d, const float* params, float* grads, const flo
         const float2* T2 = at<float2>(ws, L.t2) + (size_t)l * B * NM * W;
         TT_TRY(launch_wgrad<S>(B, dz, v(l), grads + P.Wl[l], grads + P.bl[l], err, st));
         TT_TRY(launch_rowdft<S>(dz, (long long)B * W * S, at<void>(ws, L.g), row, err, st));
-        fno_ydft_kernel<S><<<B * W, 256, 0, st>>>(row, tw, dU);
+        fno_ydft_kernel<S><<<B * W, kYdftThreads, 0, st>>>(row, tw, dU);
         TT_TRY(tt::launch_status("fno_ydft_kernel"));
         fno_specmix_bwd_kernel<<<NM, 256, 0, st>>>(B, reinterpret_cast<const float2*>(params + P.Rl[l]), T2, dU, dT2,
                                                    reinterpret_cast<float2*>(grads + P.Rl[l]));
         TT_TRY(tt::launch_status("fno_specmix_bwd_kernel"));
-        fno_iydft_kernel<S><<<B * W, 256, 0, st>>>(dT2, tw, row);
+        fno_iydft_kernel<S><<<B * W, 2 * S, 0, st>>>(dT2, tw, row);
         TT_TRY(tt::launch_status("fno_iydft_kernel"));
         TT_TRY((launch_mix<S, 1>(B, dz, at<bf16>(ws, L.wpack) + (size_t)l * 2 * W * W + W * W, at<void>(ws, L.fx), row,
                                  nullptr, l > 0 ? z(l - 1) : nullptr, nxt, nullptr, err, st)));

@@ -593,8 +593,9 @@ __global__ void __launch_bounds__(kMarchThreads) march_staged_kernel(const float
             }
         }
     }
-    auto issue = [&](int pl) {
-        if (pl < nz) {
+    // planes a..b (those below nz) as one cp.async group
+    auto issue = [&](int a, int b) {
+        for (int pl = a; pl <= b && pl < nz; ++pl) {
             float* dst = ring + (pl & (kMarchRing - 1)) * kMarchPlane;
             const float* src = qt + (size_t)pl * plane;
 #pragma unroll
@@ -604,27 +605,44 @@ __global__ void __launch_bounds__(kMarchThreads) march_staged_kernel(const float
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
 
-    for (int pl = 0; pl < kMarchRing - 2; ++pl) issue(pl);
+    // The ray's cell (i, j) and fractions (fx, fy) in [0, 1) are kept as they
+    // are; the cell, its in-grid flag and its place in the staged window are
+    // recomputed only when the ray crosses a cell face.
     MarchRay r;
-    r.u = (float)(((pi + 0.5) / P) * (nx - 1));
-    r.v = (float)(((pj + 0.5) / P) * (ny - 1));
-    for (int k = 0; k < nz; ++k) {
-        // planes k-1..k+1 must be in the ring: all but the newest kMarchRing - 4 groups done
-        asm volatile("cp.async.wait_group %0;" ::"n"(kMarchRing - 4) : "memory");
-        __syncthreads();
-        issue(k + kMarchRing - 2);  // into the slot of plane k - 2, which no step reads any more
-        if (!active) continue;
-        if (k > 0) march_kick_drift(r, mc.hz, mc);
-        int i, j;
-        float fx, fy;
+    int i = 0, j = 0, b = 0;
+    bool in = false, st = false;
+    float fx = (float)(((pi + 0.5) / P) * (nx - 1)), fy = (float)(((pj + 0.5) / P) * (ny - 1));
+    auto relocate = [&]() {
+        const float flx = floorf(fx), fly = floorf(fy);
+        i += (int)flx;
+        fx -= flx;
+        j += (int)fly;
+        fy -= fly;
+        if (fx >= 1.f) fx -= 1.f, ++i;  // a tiny negative fraction rounds up to 1
+        if (fy >= 1.f) fy -= 1.f, ++j;
+        if (i == nx - 1 && fx == 0.f) i = nx - 2, fx = 1.f;  // the grid's upper faces belong to the last cell
+        if (j == ny - 1 && fy == 0.f) j = ny - 2, fy = 1.f;
+        in = i >= 0 && i <= nx - 2 && j >= 0 && j <= ny - 2;
+        // stencil rows x = i-1..i+2 -> R = i..i+3, columns y = j-1..j+2 -> C = j+kPadY-1..j+kPadY+2
+        const int R = i + 1, C = j + kPadY;
+        st = in && R - 1 >= vR0 && R + 2 < vR1 && C - 1 >= vC0 && C + 2 < vC1;
+        b = (R - R0) * kMarchRY + (C - C0);
+    };
+    relocate();
+    const float hh = 0.5f * mc.hz, dxi = mc.hz * mc.ihx, dyi = mc.hz * mc.ihy;
+    auto step = [&](int k) {
+        if (k > 0) {  // half kick, drift to plane k
+            r.tx = fmaf(hh, r.ax, r.tx);
+            r.ty = fmaf(hh, r.ay, r.ty);
+            fx = fmaf(dxi, r.tx, fx);
+            fy = fmaf(dyi, r.ty, fy);
+            if (!(fx >= 0.f && fx < 1.f && fy >= 0.f && fy < 1.f)) relocate();
+        }
         PlaneSample s{0.f, 0.f, 0.f, 0.f};
-        if (locate(r.u, r.v, nx, ny, i, j, fx, fy)) {
-            // stencil rows x = i-1..i+2 -> R = i..i+3, columns y = j-1..j+2 -> C = j+kPadY-1..j+kPadY+2
-            const int R = i + 1, C = j + kPadY;
-            if (R - 1 >= vR0 && R + 2 < vR1 && C - 1 >= vC0 && C + 2 < vC1) {
+        if (in) {
+            if (st) {
                 const int km = k > 0 ? k - 1 : k, kp = k + 1 < nz ? k + 1 : k;
                 const float dz = (k > 0 && k + 1 < nz) ? 0.5f : 1.f;
-                const int b = (R - R0) * kMarchRY + (C - C0);
                 s = sample_node(ring + (k & (kMarchRing - 1)) * kMarchPlane + b,
                                 ring + (km & (kMarchRing - 1)) * kMarchPlane + b,
                                 ring + (kp & (kMarchRing - 1)) * kMarchPlane + b, Imm<kMarchRY>{}, dz, fx, fy);
@@ -636,6 +654,22 @@ __global__ void __launch_bounds__(kMarchThreads) march_staged_kernel(const float
             march_start(r, s, mc);
         else
             march_kick(r, mc.hz, s, mc);
+    };
+
+    // Two planes per barrier.  Groups: {0}, {1, 2}, {3, 4} ahead, then {k+5, k+6}
+    // at step pair k into the slots of planes k-3 and k-2; at pair k the ring
+    // holds planes k-3..k+4 and the pair reads k-1..k+2.
+    static_assert(kMarchRing == 8, "ring schedule below assumes 8 planes");
+    issue(0, 0);
+    issue(1, 2);
+    issue(3, 4);
+    for (int k = 0; k < nz; k += 2) {
+        asm volatile("cp.async.wait_group 1;" ::: "memory");  // all but {k+3, k+4}: planes <= k+2 are in
+        __syncthreads();
+        issue(k + 5, k + 6);
+        if (!active) continue;
+        step(k);
+        if (k + 1 < nz) step(k + 1);
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     if (active) march_write(r, k0, P * P, pi * P + pj, out);

@@ -180,16 +180,22 @@ __global__ void __launch_bounds__(128) fno_rowdft_kernel(const bf16* __restrict_
     const uint32_t idesc = U::idesc_bf16(128, NJ);
     const long long ntiles = rows / 128;
     uint32_t phase = 0;
-    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    // The A tile goes straight from global to shared memory with cp.async, all
+    // of a thread's 16-byte pieces in flight at once; the next tile's copies
+    // are issued as soon as the MMAs have read the current one, under the
+    // epilogue.  8 consecutive threads fill one core matrix (8 rows x 16 B); a
+    // warp reads 64 contiguous bytes from each of 8 rows.
+    auto stage = [&](long long t) {
         const bf16* src = in + t * 128 * (long long)S;
-        // 8 consecutive threads fill one core matrix (8 rows x 16 B): conflict-free
-        // stores; a warp reads 64 contiguous bytes from each of 8 rows
-#pragma unroll 8
         for (int q = tid; q < 128 * KG; q += 128) {
             const int r8 = q & 7, kg = (q >> 3) % KG, rg = (q >> 3) / KG;
-            const uint4 val = __ldg(reinterpret_cast<const uint4*>(src + (size_t)(rg * 8 + r8) * S + kg * 8));
-            *reinterpret_cast<uint4*>(sA + (rg * KG + kg) * 128 + r8 * 16) = val;
+            U::cp_async16(sA + (rg * KG + kg) * 128 + r8 * 16, src + (size_t)(rg * 8 + r8) * S + kg * 8);
         }
+        U::cp_async_commit();
+    };
+    if ((long long)blockIdx.x < ntiles) stage(blockIdx.x);
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        U::cp_async_wait_all();
         U::fence_proxy_async();
         __syncthreads();
         if (tid == 0) {
@@ -209,6 +215,7 @@ __global__ void __launch_bounds__(128) fno_rowdft_kernel(const bf16* __restrict_
         phase ^= 1u;
         __syncthreads();
         if (*abort_flag) break;
+        if (t + gridDim.x < ntiles) stage(t + gridDim.x);  // the MMAs are done with sA
         U::fence_after();
         float v[32];
         U::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), v);
@@ -218,6 +225,7 @@ __global__ void __launch_bounds__(128) fno_rowdft_kernel(const bf16* __restrict_
         U::fence_before();
         __syncthreads();
     }
+    U::cp_async_wait_all();  // nothing left in flight (an aborted loop can leave a stage)
     __syncthreads();
     if (warp == 0) U::tmem_dealloc(tmem, 32);
 }

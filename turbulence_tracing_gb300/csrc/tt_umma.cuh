@@ -121,6 +121,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
     return true;
 }
 
+// 16-byte global -> shared copy (cp.async, L2 only); both addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // 32 lanes x 32 consecutive columns of FP32 from TMEM (lane = this thread's row).
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
 {

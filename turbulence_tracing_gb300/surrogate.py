@@ -312,25 +312,30 @@ class _Slot:
         self.D_host = torch.ones(batch, dtype=torch.float64).pin_memory()
         self.est = torch.empty(batch, dtype=torch.float32, device=dev)
         self.est_host = torch.empty(batch, dtype=torch.float32).pin_memory()
-        self.ready = torch.cuda.Event()
+        self.marched = torch.cuda.Event()  # the slot's maps are written
+        self.ready = torch.cuda.Event()    # its estimates and kept intensities are out
         self.graph = None
+        self.keep = []
 
 
 class Pipeline:
     """Surrogate with fallback, a chunk of fields at a time: one batched march
-    over the chunk (marched and straight-line maps), then one CUDA-graph replay
-    of the rest -- encoding, network, decoding, the two shadowgrams of every
-    field (network and march) and the error estimates -- whose estimates
-    come back to the host asynchronously while the next chunk already runs
-    (two chunks in flight); the fields whose estimate exceeds tol are traced
-    exactly.  The detector drift D of each field is part of its detector
-    set-up (given)."""
+    over the chunk (marched and straight-line maps) on the march stream, then
+    one CUDA-graph replay of the rest -- encoding, network, decoding, the two
+    shadowgrams of every field (network and march) and the error estimates --
+    on the network stream, so the network of one chunk runs beside the march
+    of the next (two chunks in flight, ordered by events); the estimates come
+    back to the host asynchronously and the fields whose estimate exceeds tol
+    are traced exactly.  The detector drift D of each field is part of its
+    detector set-up (given)."""
 
     def __init__(self, W, net, kappa, tol=0.02, batch=8, graph=True):
         self.W, self.net, self.kappa, self.tol, self.B = W, net, kappa, tol, batch
         self.ws = torch.empty(core.march_batched_workspace_bytes(batch, (W.S, W.S, W.S)), dtype=torch.uint8,
                               device=W.dev)
         self.slots = [_Slot(W, batch), _Slot(W, batch)]
+        self.s_march = torch.cuda.Stream()
+        self.s_net = torch.cuda.Stream()
         for sl in self.slots:
             self._post(sl)
             torch.cuda.synchronize()
@@ -357,16 +362,23 @@ class Pipeline:
                   self.kappa, out=sl.est)
 
     def _launch(self, sl, chunk, D):
+        """Queue a chunk: the slot is free (its previous chunk's results were
+        read by the host), so the march may overwrite it."""
         W, n = self.W, len(chunk)
         sl.D_host[:n] = torch.as_tensor(D, dtype=torch.float64)
-        sl.D.copy_(sl.D_host, non_blocking=True)
-        core.march_maps_batched(chunk, W.x, W.x, W.x, W.S, lwl=W.lwl, out=sl.mar[:n], ws=self.ws)
-        if sl.graph is not None:
-            sl.graph.replay()
-        else:
-            self._post(sl)
-        sl.est_host.copy_(sl.est, non_blocking=True)
-        sl.ready.record()
+        with torch.cuda.stream(self.s_march):
+            sl.D.copy_(sl.D_host, non_blocking=True)
+            core.march_maps_batched(chunk, W.x, W.x, W.x, W.S, lwl=W.lwl, out=sl.mar[:n], ws=self.ws)
+            sl.marched.record()
+        with torch.cuda.stream(self.s_net):
+            self.s_net.wait_event(sl.marched)
+            if sl.graph is not None:
+                sl.graph.replay()
+            else:
+                self._post(sl)
+            sl.est_host.copy_(sl.est, non_blocking=True)
+            sl.keep = [sl.I_n[i].clone() for i in range(n)]
+            sl.ready.record()
 
     def run(self, fields, Ds):
         """fields: list of density tensors, Ds: their drifts.  Returns
@@ -376,14 +388,16 @@ class Pipeline:
         I_out, fell = [], []
         if not chunks:
             return I_out, fell
+        torch.cuda.current_stream().synchronize()  # fields made on the caller's stream
         self._launch(self.slots[0], *chunks[0])
         for c, (chunk, D) in enumerate(chunks):
             sl = self.slots[c % 2]
             n = len(chunk)
-            keep = [sl.I_n[i].clone() for i in range(n)]  # before the slot is reused
             if c + 1 < len(chunks):
+                # the other slot's previous chunk was read at iteration c - 1
                 self._launch(self.slots[(c + 1) % 2], *chunks[c + 1])
             sl.ready.synchronize()
+            keep = sl.keep
             est = sl.est_host[:n].tolist()
             for i in range(n):
                 if est[i] > self.tol:

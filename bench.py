@@ -682,7 +682,7 @@ def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
     units, sec = across_ranks(tot / k, sec, dist, dev)
     Np = s0_host.shape[1]
     h2d = Np * 6 * 8 + 3 * Np * 4 * 8 + Np * 8          # s0; rf re-uploaded by each diagnostic; phase weights
-    d2h = Np * (6 + 4 + 1) * 8 + Np * 2 * 4 + 4 * det * det * 8  # sf, rf, phase; status, steps; 3 H + 1 Hw
+    d2h = Np * (4 + 1) * 8 + Np * 2 * 4 + 4 * det * det * 8  # rf, phase; status, steps; 3 H + 1 Hw (sf stays on the device until read)
     return {"value": units / sec, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "seconds_per_step": sec, "steps": k, "step_seconds": times, "timing": "median step",
             "path": "ElectronCube.solve(precision='fp32', phase=True) + Shadowgraphy, Schlieren_KE, "

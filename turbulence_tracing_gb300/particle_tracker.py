@@ -127,6 +127,24 @@ class ElectronCube:
     dndy = property(lambda self: self._host("dndy"))
     dndz = property(lambda self: self._host("dndz"))
 
+    # sf (6, Np), the final ray states: after a solve from host rays it stays on
+    # the device until first read (the diagnostics use rf), then it is the same
+    # numpy array the reference keeps.
+    @property
+    def sf(self):
+        d = self.__dict__
+        if d.get("_sf_dev") is not None:
+            d["_sf"] = core.to_host(d["_sf_dev"])
+            d["_sf_dev"] = None
+        if "_sf" not in d:
+            raise AttributeError("'ElectronCube' object has no attribute 'sf'")
+        return d["_sf"]
+
+    @sf.setter
+    def sf(self, value):
+        self.__dict__["_sf"] = value
+        self.__dict__["_sf_dev"] = None
+
     def volume32(self):
         """The FP32 brick volume for the probing direction (built on first use)."""
         if self._vol32 is None:
@@ -204,7 +222,10 @@ class ElectronCube:
         finish = time()
         print("Ray trace completed in:\t", finish - start, "s")
         conv = (lambda t_: t_) if on_device else core.to_host
-        self.sf = conv(out["sf"])
+        if on_device:
+            self.sf = out["sf"]
+        else:
+            self.__dict__["_sf_dev"] = out["sf"]  # copied on first read of self.sf
         self.rf = conv(out["rf"])
         self.status = conv(out["status"])
         self.nsteps = conv(out["nsteps"])
@@ -215,7 +236,12 @@ class ElectronCube:
     def ray_at_exit(self):
         """Back-project self.sf to the exit plane (particle_tracker.py:333-380); runs on the GPU."""
         dev = core.require_cuda()
-        sf = self.sf if isinstance(self.sf, torch.Tensor) else torch.as_tensor(np.asarray(self.sf), device=dev)
+        lazy = self.__dict__.get("_sf_dev")
+        host = lazy is not None or not isinstance(self.sf, torch.Tensor)
+        if lazy is not None:
+            sf = lazy
+        else:
+            sf = self.sf if isinstance(self.sf, torch.Tensor) else torch.as_tensor(np.asarray(self.sf), device=dev)
         sf = sf.to(device=dev, dtype=torch.float64)
         x, y, z, vx, vy, vz = sf
         extent = self._extent()
@@ -229,7 +255,7 @@ class ElectronCube:
         elif self.probing_direction == "z":
             t_bp = (z - extent) / vz
             rp[0], rp[2], rp[1], rp[3] = x - vx * t_bp, y - vy * t_bp, torch.atan(vx / vz), torch.atan(vy / vz)
-        if isinstance(self.sf, torch.Tensor):
+        if not host:
             return rp
         return rp.cpu().numpy()
 
@@ -247,6 +273,8 @@ class ElectronCube:
 
     # --- pickling (the reference's multiprocess driver pickles bound methods)
     def __getstate__(self):
+        if self.__dict__.get("_sf_dev") is not None:
+            self.sf  # bring the final states to the host before pickling
         st = dict(self.__dict__)
         st["_dev"] = None
         st["_vol32"] = None

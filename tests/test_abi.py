@@ -87,3 +87,43 @@ def test_no_gpu_means_loud_failure():
 
     with pytest.raises(RuntimeError, match="CUDA"):
         core.calc_dndr(np.zeros((4, 4, 4)), np.arange(4.0), np.arange(4.0), np.arange(4.0))
+
+
+def test_march_and_shadowgram_arguments_checked_before_any_launch():
+    """Invalid calls are refused by the library's own checks (no CUDA call is
+    made), with the status and a detail string."""
+    import ctypes
+
+    from turbulence_tracing_gb300 import _lib
+
+    L = _lib.lib(build_if_missing=False)
+    x = np.linspace(0.0, 1e-3, 8)
+    dp = ctypes.POINTER(ctypes.c_double)
+    xp = x.ctypes.data_as(dp)
+    fake = ctypes.c_void_p(0x1000)  # never dereferenced: every call below fails its checks first
+    assert L.tt_march_maps_workspace_bytes(1, 8, 8) == 0
+    need = L.tt_march_maps_workspace_bytes(8, 8, 8)
+    assert need > 8 * 8 * 8 * 4
+    assert L.tt_march_maps_batched_workspace_bytes(3, 8, 8, 8) >= 3 * need - 3 * 256
+    cases = [
+        (lambda: L.tt_march_maps(None, _lib.TT_F32, 8, 8, 8, xp, xp, xp, 1e-6, 1.0, 8, fake, fake, need, None),
+         b"NULL"),
+
+        (lambda: L.tt_march_maps(fake, _lib.TT_F32, 8, 8, 1, xp, xp, xp, 1e-6, 1.0, 8, fake, fake, need, None),
+         b"bad sizes"),
+        (lambda: L.tt_march_maps(fake, 7, 8, 8, 8, xp, xp, xp, 1e-6, 1.0, 8, fake, fake, need, None), b"ne_dtype"),
+        (lambda: L.tt_march_maps(fake, _lib.TT_F32, 8, 8, 8, xp, xp, xp, 1e-6, 1.0, 8, fake,
+                                 ctypes.c_void_p(0x1004), need, None), b"aligned"),
+        (lambda: L.tt_march_maps_batched((ctypes.c_void_p * 1)(fake), 0, _lib.TT_F32, 8, 8, 8, xp, xp, xp, 1e-6, 1.0,
+                                         8, fake, fake, need, None), b"fields"),
+        (lambda: L.tt_march_maps_batched((ctypes.c_void_p * 33)(*([fake] * 33)), 33, _lib.TT_F32, 8, 8, 8, xp, xp, xp,
+                                         1e-6, 1.0, 8, fake, fake, 33 * need, None), b"fields"),
+        (lambda: L.tt_shadowgram_batched(fake, 0, 8, 1e-5, fake, fake, None), b"bad arguments"),
+        (lambda: L.tt_shadowgram_batched(fake, 2, 1, 1e-5, fake, fake, None), b"bad arguments"),
+        (lambda: L.tt_shadowgram_batched(fake, 2, 8, 0.0, fake, fake, None), b"bad arguments"),
+    ]
+    for call, detail in cases:
+        assert call() == 1  # invalid argument
+        assert detail in L.tt_last_error_detail(), L.tt_last_error_detail()
+    assert L.tt_march_maps(fake, _lib.TT_F32, 8, 8, 8, xp, xp, xp, 1e-6, 1.0, 8, fake, fake, need - 4, None) == 2
+    assert b"workspace needs" in L.tt_last_error_detail()

@@ -114,6 +114,23 @@ def test_march_maps_match_restatement(cuda, n, P):
     assert np.abs(m[0] - st[0]).max() > 1e-2 * scale
 
 
+@pytest.mark.parametrize("n,P", [(2, 1), (2, 3), (3, 2), (3, 1), (4, 64)])
+def test_march_smallest_grids(cuda, n, P):
+    """Two- and three-node axes (every stencil on the ghost border), a single
+    ray, and pixel grids far finer than the node grid."""
+    from turbulence_tracing_gb300 import core
+
+    rng = np.random.default_rng(100 * n + P)
+    ne = 1e25 * (1.0 + 0.2 * rng.standard_normal((n, n, n)))
+    x = np.linspace(-0.5e-3, 0.5e-3, n)
+    m = core.march_maps(ne, x, x, x, P, lwl=1064e-9).cpu().numpy()
+    ref = _march_restated(ne, x, 1064e-9, P)
+    scale = np.abs(ref[0:2]).max()
+    for c in (0, 1, 3, 4):
+        assert np.abs(m[c] - ref[c]).max() <= 1e-4 * scale, c
+    assert np.abs(m[2] - ref[2]).max() <= 1e-4 * np.abs(ref[2]).max()
+
+
 def test_march_far_drift_reads_outside_the_staged_window(cuda):
     """Rays that drift further than the staged halo (8 cells) take their
     samples from global memory; the answer is the same."""

@@ -696,8 +696,11 @@ extern "C" int tt_march_maps_batched(const void* const* ne, int nfields, int ne_
     if (nfields < 1 || nfields > TT_MAX_MARCH_FIELDS) return tt::invalid("march_maps: 1..TT_MAX_MARCH_FIELDS fields");
     if (nx < 2 || ny < 2 || nz < 2 || P < 1 || (long long)P * P > 0x7fffffffLL / 5 || nx > 65535 || ny > 65535 * 32)
         return tt::invalid("march_maps: bad sizes");
-    if (workspace_bytes < tt_march_maps_batched_workspace_bytes(nfields, nx, ny, nz))
-        return tt::invalid("march_maps: workspace too small");
+    const size_t need = tt_march_maps_batched_workspace_bytes(nfields, nx, ny, nz);
+    if (workspace_bytes < need) {
+        tt::set_detail("march_maps: workspace needs %zu bytes", need);
+        return TT_ERR_WORKSPACE_TOO_SMALL;
+    }
     if (ne_dtype != TT_F32 && ne_dtype != TT_F64) return tt::invalid("march_maps: ne_dtype");
     if ((reinterpret_cast<uintptr_t>(workspace) & 15) != 0) return tt::invalid("march_maps: workspace not 16-byte aligned");
     MarchFields fields{};

@@ -31,25 +31,28 @@ def _maps_restated(ne, x, lwl, S):
     return -0.5 * (bil(gx) * w).sum(-1), -0.5 * (bil(gy) * w).sum(-1)
 
 
-def _march_restated(ne, x, lwl, P):
+def _march_restated(ne, x, lwl, P, y=None, z=None):
     """The plane march in float64: q = min(ne/n_c, 1), numpy.gradient
     derivatives, bilinear on the node planes (zero outside the grid), and
     kick-drift-kick in z from plane to plane on the ray equation, the closing
     kick's slope-dependent term at the slope predicted with the previous
     step's acceleration; trapezoid phase in ds.
     Then the straight ray from the same pixel centre: trapezoid deflection
-    integrals on the planes."""
+    integrals on the planes.  Uniform axes x, y, z (y and z default to x)."""
+    y = x if y is None else y
+    z = x if z is None else z
     omega, nc = R.critical_density(lwl)
     q = np.minimum(ne / nc, 1.0)
-    n, h = len(x), x[1] - x[0]
-    fields = (q, np.gradient(q, axis=0) / h, np.gradient(q, axis=1) / h, np.gradient(q, axis=2) / h)
-    c = (np.arange(P) + 0.5) / P * (n - 1)
-    u, v = np.repeat(c, P), np.tile(c, P)
+    nx, ny, nz = q.shape
+    hx, hy, hz = x[1] - x[0], y[1] - y[0], z[1] - z[0]
+    fields = (q, np.gradient(q, axis=0) / hx, np.gradient(q, axis=1) / hy, np.gradient(q, axis=2) / hz)
+    u = np.repeat((np.arange(P) + 0.5) / P * (nx - 1), P)
+    v = np.tile((np.arange(P) + 0.5) / P * (ny - 1), P)
 
     def sample(u, v, k):
-        ins = (u >= 0) & (u <= n - 1) & (v >= 0) & (v <= n - 1)
-        i = np.clip(np.floor(np.where(ins, u, 0)).astype(int), 0, n - 2)
-        j = np.clip(np.floor(np.where(ins, v, 0)).astype(int), 0, n - 2)
+        ins = (u >= 0) & (u <= nx - 1) & (v >= 0) & (v <= ny - 1)
+        i = np.clip(np.floor(np.where(ins, u, 0)).astype(int), 0, nx - 2)
+        j = np.clip(np.floor(np.where(ins, v, 0)).astype(int), 0, ny - 2)
         fx, fy = np.where(ins, u, 0) - i, np.where(ins, v, 0) - j
         out = []
         for F in fields:
@@ -72,10 +75,10 @@ def _march_restated(ne, x, lwl, P):
     tx, ty = np.zeros_like(u), np.zeros_like(u)
     ax, ay = accel(f, tx, ty, q0)
     e, phi = dphase(f, tx, ty), np.zeros_like(u)
-    for k in range(1, n):
-        d = h
+    for k in range(1, nz):
+        d = hz
         tx, ty = tx + d / 2 * ax, ty + d / 2 * ay
-        u, v = u + tx, v + ty
+        u, v = u + d / hx * tx, v + d / hy * ty
         f = sample(u, v, k)
         ax, ay = accel(f, tx + d / 2 * ax, ty + d / 2 * ay, q0)
         tx, ty = tx + d / 2 * ax, ty + d / 2 * ay
@@ -85,12 +88,35 @@ def _march_restated(ne, x, lwl, P):
     k0 = omega / R.C_LIGHT
     # the straight ray
     sxs, sys_ = np.zeros_like(u), np.zeros_like(u)
-    for k in range(n):
+    for k in range(nz):
         f = sample(u0, v0, k)
-        w = 0.5 if k in (0, n - 1) else 1.0
+        w = 0.5 if k in (0, nz - 1) else 1.0
         sxs += w * f[1]
         sys_ += w * f[2]
-    return np.stack([np.arctan(tx), np.arctan(ty), k0 * phi, -0.5 * h * sxs, -0.5 * h * sys_]).reshape(5, P, P)
+    return np.stack([np.arctan(tx), np.arctan(ty), k0 * phi, -0.5 * hz * sxs, -0.5 * hz * sys_]).reshape(5, P, P)
+
+
+@pytest.mark.parametrize("P", [40, 20])
+def test_march_non_cubic_grid(cuda, P):
+    """nx, ny, nz and their spacings all different (P = 40: staged tiles; P = 20
+    is coarser than both transverse grids: the unstaged kernel)."""
+    from turbulence_tracing_gb300 import core
+
+    rng = np.random.default_rng(P)
+    nx, ny, nz = 40, 28, 33
+    x = np.linspace(-0.6e-3, 0.6e-3, nx)
+    y = np.linspace(-0.5e-3, 0.5e-3, ny)
+    z = np.linspace(-0.4e-3, 0.4e-3, nz)
+    g = rng.standard_normal((nx, ny, nz))
+    ne = 2e25 * (1.0 + 0.2 * g)
+    m = core.march_maps(ne, x, y, z, P, lwl=1064e-9).cpu().numpy()
+    ref = _march_restated(ne, x, 1064e-9, P, y, z)
+    scale = np.abs(ref[0:2]).max()
+    for c in (0, 1, 3, 4):
+        assert np.abs(m[c] - ref[c]).max() <= 1e-4 * scale, c
+    assert np.abs(m[2] - ref[2]).max() <= 1e-4 * np.abs(ref[2]).max()
+    st = core.straight_line_maps(ne, x, y, z, P, lwl=1064e-9).cpu().numpy()
+    assert np.abs(m[3:5] - st[0:2]).max() <= 1e-5 * scale
 
 
 @pytest.mark.parametrize("n,P", [(40, 32), (40, 40), (44, 60), (48, 47), (48, 24)])

@@ -33,6 +33,10 @@ per field from the straight-line map so the contrast is 20%); the error of a
 prediction is ||I_pred - I_trace||_2 / ||I_trace||_2.  The error estimate is
 kappa * ||I_net - I_march|| / ||I_net|| (how far the network moved the
 answer), kappa calibrated on held-out fields so that 90% of them are bounded.
+
+Pipeline runs many fields in chunks (batched march, graph-captured network
+and estimates, two streams); TileScreen screens one large field per 256^2 tile
+and re-traces only the flagged tiles' pixel rays.
 """
 import math
 import time

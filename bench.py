@@ -76,6 +76,7 @@ def parse():
     ap.add_argument("--sur-test", type=int, default=96)
     ap.add_argument("--sur-epochs", type=int, default=15)
     ap.add_argument("--sur-batch", type=int, default=16, help="fields per chunk in the surrogate pipeline")
+    ap.add_argument("--sur-time", type=int, default=96, help="fresh fields for timing the pipeline")
     ap.add_argument("--no-screen", action="store_true", help="skip the per-tile screening of the stress field")
     ap.add_argument("--screen-n", type=int, default=1024, help="stress-field grid for the tile screening leg")
     ap.add_argument("--screen-train", type=int, default=8, help="training fields (16 tiles each at 1024^3)")
@@ -521,9 +522,8 @@ def surrogate_run(a):
     fwd_bytes = 4 * (6 * C * S * S * 1 + 16 * C * 32 * S) + (4 * W.in_ch + 2 * C) * S * S + (2 * C + 12) * S * S
     march_bytes = 4 * S ** 3 * 3 + 20 * S * S  # density read, plane-major q written and read once, 5 maps
     peak, peak_kind = peaks()
-    # the pipeline against tracing every held-out field
-    params = SG.draw_fields(a.sur_test, seed=a.seed + 12)[half:]
-    fields = [W.field(p) for p in params]
+    # the pipeline against tracing every field, on fresh fields drawn the same way
+    fields = [W.field(p) for p in SG.draw_fields(a.sur_time, seed=a.seed + 15)]
     # detector set-up: each field's drift for 20% straight-line contrast
     Ds = [float(W.drift(W.maps(f))) for f in fields]
     pipe = SG.Pipeline(W, net, kappa, batch=a.sur_batch)
@@ -547,7 +547,8 @@ def surrogate_run(a):
     errs = [SG.rel_l2(p_, t_) for p_, t_ in zip(I_p, I_t)]
     acc = [e for e, f in zip(errs, fell) if not f]
     bt_dev = max(SG.rel_l2(b_, t_) for b_, t_ in zip(I_b, I_t))
-    return {"grid": S, "train_fields": a.sur_train, "test_fields": a.sur_test, "epochs": a.sur_epochs,
+    return {"grid": S, "train_fields": a.sur_train, "test_fields": a.sur_test, "timed_fields": len(fields),
+            "epochs": a.sur_epochs,
             "data_s": t_data, "train_samples_per_s": sps, "loss_first_last": [hist[0], hist[-1]],
             "target_rms": target_rms,
             "heldout": {"shadow_err_straight": mean("err_straight"), "shadow_err_march": mean("err_march"),

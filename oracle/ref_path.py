@@ -119,6 +119,9 @@ def main(argv=None):
     ap.add_argument("--lwl", type=float, default=1064e-9)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--procs", type=int, default=0)
+    ap.add_argument("--rtol", type=float, default=1e-3, help="solve_ivp rtol (the reference's default 1e-3)")
+    ap.add_argument("--atol", type=float, default=1e-6, help="solve_ivp atol (the reference's default 1e-6)")
+    ap.add_argument("--bundle", type=int, default=0, help="rays per solve_ivp call (0: rays / procs)")
     ap.add_argument("--json", required=True)
     a = ap.parse_args(argv)
     ne = np.load(a.density, mmap_mode="r")
@@ -129,9 +132,10 @@ def main(argv=None):
     t_setup = time.perf_counter() - t0
     s0 = R.gaussian_beam(a.rays, a.sigma, a.div, x.max(), np.random.default_rng(a.seed))
     nproc = a.procs or host_cores()
-    r = run_pool(cube, s0, R.t_end(x.max()), nproc)
+    r = run_pool(cube, s0, R.t_end(x.max()), nproc, bundle=a.bundle or None, rtol=a.rtol, atol=a.atol)
     out = dict(ray_steps=r["ray_steps"], wall=r["wall"], rays=a.rays, procs=nproc, setup_s=t_setup,
-               ray_steps_per_s=r["ray_steps"] / r["wall"], rays_per_s=a.rays / r["wall"])
+               ray_steps_per_s=r["ray_steps"] / r["wall"], rays_per_s=a.rays / r["wall"], rtol=a.rtol, atol=a.atol,
+               bundle=a.bundle or -(-a.rays // nproc))
     with open(a.json, "w") as f:
         json.dump(out, f)
     print(json.dumps(out))

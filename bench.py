@@ -62,7 +62,7 @@ def parse():
     ap.add_argument("--det", type=int, default=1024)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--fp64-rays", type=int, default=20000)
-    ap.add_argument("--check-rays", type=int, default=2000)
+    ap.add_argument("--check-rays", type=int, default=20000)
     ap.add_argument("--cpu-rays", type=int, default=8000)
     ap.add_argument("--cpu-bar-rays", type=int, default=128, help="CPU sample at the accuracy-bar tolerance")
     ap.add_argument("--ref-rays", type=int, default=8000)

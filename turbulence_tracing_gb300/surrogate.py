@@ -339,7 +339,8 @@ class Pipeline:
                               device=W.dev)
         self.slots = [_Slot(W, batch), _Slot(W, batch)]
         self.s_march = torch.cuda.Stream()
-        self.s_net = torch.cuda.Stream()
+        # the network's small, latency-bound kernels go first when SM slots free up
+        self.s_net = torch.cuda.Stream(priority=-1)
         for sl in self.slots:
             self._post(sl)
             torch.cuda.synchronize()

@@ -556,6 +556,24 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
                  : "memory");
 }
 
+template <int V>
+struct Slot {  // a ring slot known at compile time
+    static constexpr int value = V;
+};
+
+// The march's out-of-line sampler: the first and last planes from the ring
+// (d/dz one-sided there) and rays whose stencil has left the staged window
+// (from the padded volume in global memory).
+__device__ __noinline__ PlaneSample sample_slow(const float* ring, bool staged, int b, const float* __restrict__ qt,
+                                                int nx, int ny, int nz, int i, int j, float fx, float fy, int k)
+{
+    if (!staged) return sample_global(qt, nx, ny, nz, i, j, fx, fy, k);
+    const int km = k > 0 ? k - 1 : k, kp = k + 1 < nz ? k + 1 : k;
+    const float dz = (k > 0 && k + 1 < nz) ? 0.5f : 1.f;
+    return sample_node(ring + (k & (kMarchRing - 1)) * kMarchPlane + b, ring + (km & (kMarchRing - 1)) * kMarchPlane + b,
+                       ring + (kp & (kMarchRing - 1)) * kMarchPlane + b, Imm<kMarchRY>{}, dz, fx, fy);
+}
+
 // Pixel grids at least as fine as the node grid (a tile spans at most
 // kMarchRows x kMarchCols node cells).  Window coordinates are padded ones:
 // row R = x + 1, column C = y + kPadY.
@@ -630,8 +648,15 @@ __global__ void __launch_bounds__(kMarchThreads) march_staged_kernel(const float
     };
     relocate();
     const float hh = 0.5f * mc.hz, dxi = mc.hz * mc.ihx, dyi = mc.hz * mc.ihy;
-    auto step = [&](int k) {
-        if (k > 0) {  // half kick, drift to plane k
+    // Step to plane k, whose ring slot K = k mod kMarchRing is a compile-time
+    // constant: inside the volume the stencil's three planes sit at fixed
+    // offsets from the ray's window base, so its shared loads need no address
+    // arithmetic.  The first and last planes (one-sided d/dz) and rays outside
+    // the staged window take the out-of-line sampler.
+    auto step = [&](int k, auto slot) {
+        constexpr int K = decltype(slot)::value;
+        const bool first = K == 0 && k == 0;
+        if (!first) {  // half kick, drift to plane k
             r.tx = fmaf(hh, r.ax, r.tx);
             r.ty = fmaf(hh, r.ay, r.ty);
             fx = fmaf(dxi, r.tx, fx);
@@ -640,36 +665,62 @@ __global__ void __launch_bounds__(kMarchThreads) march_staged_kernel(const float
         }
         PlaneSample s{0.f, 0.f, 0.f, 0.f};
         if (in) {
-            if (st) {
-                const int km = k > 0 ? k - 1 : k, kp = k + 1 < nz ? k + 1 : k;
-                const float dz = (k > 0 && k + 1 < nz) ? 0.5f : 1.f;
-                s = sample_node(ring + (k & (kMarchRing - 1)) * kMarchPlane + b,
-                                ring + (km & (kMarchRing - 1)) * kMarchPlane + b,
-                                ring + (kp & (kMarchRing - 1)) * kMarchPlane + b, Imm<kMarchRY>{}, dz, fx, fy);
+            if (st && !first && k + 1 < nz) {
+                const float* c = ring + b;
+                s = sample_node(c + K * kMarchPlane, c + ((K + kMarchRing - 1) % kMarchRing) * kMarchPlane,
+                                c + ((K + 1) % kMarchRing) * kMarchPlane, Imm<kMarchRY>{}, 0.5f, fx, fy);
             } else {
-                s = sample_global(qt, nx, ny, nz, i, j, fx, fy, k);
+                s = sample_slow(ring, st, b, qt, nx, ny, nz, i, j, fx, fy, k);
             }
         }
-        if (k == 0)
+        if (first)
             march_start(r, s, mc);
         else
             march_kick(r, mc.hz, s, mc);
     };
-
+    // planes pl and pl + 1 (those below nz) into ring slots S and S + 1, one group
+    auto issue2 = [&](int pl, auto slot) {
+        constexpr int S = decltype(slot)::value;
+        if (pl < nz) {
+            const float* src = qt + (size_t)pl * plane;
+#pragma unroll
+            for (int q = 0; q < kMarchChunksPerThread; ++q)
+                if (soff[q] >= 0) cp_async16(ring + S * kMarchPlane + soff[q], src + goff[q]);
+        }
+        if (pl + 1 < nz) {
+            const float* src = qt + (size_t)(pl + 1) * plane;
+#pragma unroll
+            for (int q = 0; q < kMarchChunksPerThread; ++q)
+                if (soff[q] >= 0) cp_async16(ring + ((S + 1) % kMarchRing) * kMarchPlane + soff[q], src + goff[q]);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
     // Two planes per barrier.  Groups: {0}, {1, 2}, {3, 4} ahead, then {k+5, k+6}
     // at step pair k into the slots of planes k-3 and k-2; at pair k the ring
     // holds planes k-3..k+4 and the pair reads k-1..k+2.
+    auto pair = [&](int k, auto slot) {
+        constexpr int K = decltype(slot)::value;
+        asm volatile("cp.async.wait_group 1;" ::: "memory");  // all but {k+3, k+4}: planes <= k+2 are in
+        __syncthreads();
+        issue2(k + 5, Slot<(K + 5) % kMarchRing>{});
+        if (active) {
+            step(k, slot);
+            if (k + 1 < nz) step(k + 1, Slot<K + 1>{});
+        }
+    };
     static_assert(kMarchRing == 8, "ring schedule below assumes 8 planes");
     issue(0, 0);
     issue(1, 2);
     issue(3, 4);
-    for (int k = 0; k < nz; k += 2) {
-        asm volatile("cp.async.wait_group 1;" ::: "memory");  // all but {k+3, k+4}: planes <= k+2 are in
-        __syncthreads();
-        issue(k + 5, k + 6);
-        if (!active) continue;
-        step(k);
-        if (k + 1 < nz) step(k + 1);
+    // four pairs per pass, so every ring slot is a constant
+    for (int k = 0; k < nz; k += kMarchRing) {
+        pair(k, Slot<0>{});
+        if (k + 2 >= nz) break;
+        pair(k + 2, Slot<2>{});
+        if (k + 4 >= nz) break;
+        pair(k + 4, Slot<4>{});
+        if (k + 6 >= nz) break;
+        pair(k + 6, Slot<6>{});
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     if (active) march_write(r, k0, P * P, pi * P + pj, out);

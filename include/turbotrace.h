@@ -332,7 +332,7 @@ int tt_shadowgram_batched(const float* theta, int nmaps, int P, double pitch, co
  * of the in_ch data channels plus two coordinate channels (row, column, each
  * (i + 0.5) 2/S - 1) to width 32, `layers` Fourier layers (truncated DFT
  * keeping 16 x 32 modes, per-mode complex 32 x 32 mixing, inverse DFT, plus a
- * 1x1 convolution and bias, then GELU), and a pointwise projection to out_ch.
+ * 1x1 convolution and bias, then GELU in its tanh form), and a pointwise projection to out_ch.
  * Activations are bfloat16 with FP32 accumulation; every contraction over
  * pixels runs on the tcgen05 tensor cores.
  *

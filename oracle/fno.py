@@ -15,7 +15,7 @@ Network (width C, retained modes m in each direction, grid S x S):
     U[o]       = sum_c R[o, c] T2[c]                       (per mode, complex)
     S1[y, kx]  = sum_ky U[ky, kx] exp(+2 pi i ky y / S)
     s[y, x]    = sum_kx c_kx Re(S1[y, kx] exp(+2 pi i kx x / S)) / S^2,  c_0 = 1, c_k = 2
-    z          = W v + b + s ;   v = GELU(z)   (erf form)
+    z          = W v + b + s ;   v = GELU(z)   (tanh form)
   out    = Q v + qb                                  (projection, per pixel)
   loss   = sum_k w_k sum (out_k - target_k)^2 / (B S^2)
 
@@ -28,7 +28,6 @@ dT1 fed to the tensor cores, and the backward activations dz.
 import math
 
 import numpy as np
-from scipy.special import erf
 
 WIDTH = 32
 MODES = 16
@@ -42,12 +41,19 @@ def bf16(x):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+GELU_A = math.sqrt(2.0 / math.pi)
+GELU_B = 0.044715
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / math.sqrt(2.0)))
+    """GELU in its tanh form (Hendrycks & Gimpel 2016):
+    z/2 (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3)))."""
+    return 0.5 * z * (1.0 + np.tanh(GELU_A * (z + GELU_B * z ** 3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    t = np.tanh(GELU_A * (z + GELU_B * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GELU_A * (1.0 + 3.0 * GELU_B * z * z)
 
 
 def ky_list(S, m=MODES):

@@ -36,11 +36,35 @@ constexpr int MD = TT_FNO_MODES;  // 16 modes per direction
 constexpr int NJ = 2 * MD;         // 32 row-spectrum columns
 constexpr int NM = 2 * MD * MD;    // 512 retained modes
 
-__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU in its tanh form (Hendrycks & Gimpel, 2016),
+//   GELU(z) = z/2 (1 + tanh(a(z))),  a(z) = sqrt(2/pi) (z + 0.044715 z^3),
+// with the hardware tanh approximation: one MUFU operation instead of an erf.
+// Its error (about 2^-11 relative in tanh) is below the bfloat16 rounding of
+// every value the kernels store.
+constexpr float kGeluA = 0.7978845608028654f;          // sqrt(2/pi)
+constexpr float kGeluB = 0.7978845608028654f * 0.044715f;
 
+__device__ __forceinline__ float tanh_approx(float x)
+{
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(x));
+    return t;
+}
+
+__device__ __forceinline__ float gelu_f(float z)
+{
+    const float t = tanh_approx(z * fmaf(kGeluB, z * z, kGeluA));
+    const float h = 0.5f * z;
+    return fmaf(h, t, h);
+}
+
+// d GELU / dz = (1 + t)/2 + z/2 (1 - t^2) a'(z),  a'(z) = sqrt(2/pi) (1 + 3 * 0.044715 z^2)
 __device__ __forceinline__ float gelu_grad_f(float z)
 {
-    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * expf(-0.5f * z * z) * 0.39894228040143268f;
+    const float z2 = z * z;
+    const float t = tanh_approx(z * fmaf(kGeluB, z2, kGeluA));
+    const float da = fmaf(3.f * kGeluB, z2, kGeluA);
+    return fmaf(0.5f, t, 0.5f) + (0.5f * z) * fmaf(-t, t, 1.f) * da;
 }
 
 __device__ __forceinline__ void flag_error(int* err)

@@ -298,19 +298,35 @@ __global__ void __launch_bounds__(128) fno_mix_kernel(int B, const bf16* __restr
     const long long ntiles = (long long)B * S * XT;
     const size_t plane = (size_t)S * S;
     uint32_t phase = 0;
+    // The global loads of tile t + gridDim.x are issued before the epilogue of
+    // tile t and land in registers while it runs; the next iteration moves them
+    // to shared memory.
+    uint4 pin[4];   // in[b, c, y, x0 + 8 xg .. + 8] for xg = 4 warp + it, c = lane
+    float4 psp[2];  // sp[b, o, y, 8 jg .. + 8] for o = tid / 4, jg = tid % 4
+    auto fetch = [&](long long t) {
+        const long long by = t / XT;
+        const int b = (int)(by / S), y = (int)(by % S);
+        const bf16* row = in + ((size_t)b * W + (tid & 31)) * plane + (size_t)y * S + x0;
+#pragma unroll
+        for (int it = 0; it < 4; ++it)
+            pin[it] = __ldg(reinterpret_cast<const uint4*>(row + ((tid >> 5) * 4 + it) * 8));
+        const float4* sv = reinterpret_cast<const float4*>(sp + (((size_t)b * W + (tid >> 2)) * S + y) * NJ +
+                                                           (tid & 3) * 8);
+        psp[0] = __ldg(sv);
+        psp[1] = __ldg(sv + 1);
+    };
+    if ((long long)blockIdx.x < ntiles) fetch(blockIdx.x);
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const long long by = t / XT;
         const int b = (int)(by / S), y = (int)(by % S);
         // A1: in[b, c, y, x0:x0+128] transposed into K-major [x][c]; each thread
-        // reads 64 contiguous bytes of one channel row
+        // holds 64 contiguous bytes of one channel row
         {
             const int c = tid & 31;
-            const bf16* row = in + ((size_t)b * W + c) * plane + (size_t)y * S + x0;
 #pragma unroll
             for (int it = 0; it < 4; ++it) {
                 const int xg = (tid >> 5) * 4 + it;  // 8-column group, 0..15
-                const uint4 val = __ldg(reinterpret_cast<const uint4*>(row + xg * 8));
-                const bf16* e = reinterpret_cast<const bf16*>(&val);
+                const bf16* e = reinterpret_cast<const bf16*>(&pin[it]);
                 uint8_t* base = sA1 + (xg * 4 + (c >> 3)) * 128 + (c & 7) * 2;
 #pragma unroll
                 for (int i = 0; i < 8; ++i) *reinterpret_cast<bf16*>(base + i * 16) = e[i];
@@ -319,8 +335,7 @@ __global__ void __launch_bounds__(128) fno_mix_kernel(int B, const bf16* __restr
         // B2: sp[b, o, y, 0:32] -> bf16 K-major [o][j]
         {
             const int o = tid >> 2, jg = tid & 3;
-            const float4* s = reinterpret_cast<const float4*>(sp + (((size_t)b * W + o) * S + y) * NJ + jg * 8);
-            const float4 p0 = __ldg(s), p1 = __ldg(s + 1);
+            const float4 p0 = psp[0], p1 = psp[1];
             __align__(16) bf16 h[8] = {__float2bfloat16_rn(p0.x), __float2bfloat16_rn(p0.y), __float2bfloat16_rn(p0.z),
                                        __float2bfloat16_rn(p0.w), __float2bfloat16_rn(p1.x), __float2bfloat16_rn(p1.y),
                                        __float2bfloat16_rn(p1.z), __float2bfloat16_rn(p1.w)};
@@ -346,12 +361,13 @@ __global__ void __launch_bounds__(128) fno_mix_kernel(int B, const bf16* __restr
         phase ^= 1u;
         __syncthreads();
         if (abort_flag) break;
+        if (t + gridDim.x < ntiles) fetch(t + gridDim.x);
         U::fence_after();
         float acc[32];
         U::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), acc);
         const int x = x0 + warp * 32 + lane;
         const size_t pix = (size_t)y * S + x;
-#pragma unroll 8
+#pragma unroll  // acc stays in registers
         for (int o = 0; o < W; ++o) {
             const size_t idx = ((size_t)b * W + o) * plane + pix;
             if (MODE == 0) {
@@ -989,7 +1005,7 @@ int launch_mix(int B, const bf16* in, const void* wpack, const void* apack, cons
                const bf16* zprev, bf16* out0, bf16* out1, int* err, cudaStream_t st)
 {
     constexpr int XT = S / 128;
-    int g = grid_for((long long)B * S * XT, 8);
+    int g = grid_for((long long)B * S * XT, 6);  // 80 registers: 6 blocks per SM
     g = (g / XT) * XT;
     if (g < XT) g = XT;
     fno_mix_kernel<S, MODE><<<g, 128, 0, st>>>(B, in, (const uint4*)wpack, (const uint4*)apack, sp, bias, zprev, out0,

@@ -24,6 +24,7 @@
 #include "tt_common.cuh"
 #include "tt_umma.cuh"
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 namespace {
@@ -172,10 +173,14 @@ __global__ void fno_pack_weights_kernel(WPackArgs a, const float* __restrict__ p
 
 // ----------------------------------------------------------------------------- rowdft (tcgen05)
 // out[r, 0:32] = sum_x in[r, x] * M[j, x] for r in [0, rows), rows % 128 == 0.
-// One 128-row tile per iteration: the tile (128 x S bf16) is staged in shared
-// memory, S/16 MMAs (M = 128, N = 32, K = 16) accumulate into 32 TMEM columns.
+// One 128-row tile per iteration: the tile (128 x S bf16) arrives in shared
+// memory by TMA, S/16 MMAs (M = 128, N = 32, K = 16) accumulate into 32 TMEM
+// columns.  The tensor map views `in` as rows of S bf16; a tile is S/8 boxes of
+// 8 columns x 128 rows, and box kg lands at sA + kg * 2048 as 16 core matrices
+// (8 rows x 16 B) stacked along the rows.  So in the A descriptor the core
+// matrices adjacent along K are 2048 B apart and the 8-row groups 128 B.
 template <int S>
-__global__ void __launch_bounds__(128) fno_rowdft_kernel(const bf16* __restrict__ in, long long rows,
+__global__ void __launch_bounds__(128) fno_rowdft_kernel(const __grid_constant__ CUtensorMap amap, long long rows,
                                                          const uint4* __restrict__ mpack, float* __restrict__ out,
                                                          int* __restrict__ err)
 {
@@ -183,17 +188,21 @@ __global__ void __launch_bounds__(128) fno_rowdft_kernel(const bf16* __restrict_
     constexpr int KG = S / 8;
     constexpr int A_BYTES = 128 * S * 2;
     constexpr int B_BYTES = NJ * S * 2;
+    constexpr int KG_BYTES = 128 * 16;  // one box: 128 rows x 8 columns
     extern __shared__ __align__(1024) uint8_t sm[];
     uint8_t* sA = sm;
     uint8_t* sB = sm + A_BYTES;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + A_BYTES + B_BYTES);
-    uint32_t* holder = reinterpret_cast<uint32_t*>(bar + 1);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + A_BYTES + B_BYTES);  // the MMAs of a tile are done
+    uint64_t* tbar = bar + 1;                                              // a tile has arrived
+    uint32_t* holder = reinterpret_cast<uint32_t*>(tbar + 1);
     int* abort_flag = reinterpret_cast<int*>(holder + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     for (int i = tid; i < B_BYTES / 16; i += 128) reinterpret_cast<uint4*>(sB)[i] = mpack[i];
+    U::fence_proxy_async();  // sB written by the threads, read by the tensor cores
     if (tid == 0) {
         U::mbar_init(bar, 1);
+        U::mbar_init(tbar, 1);
         *abort_flag = 0;
     }
     if (warp == 0) U::tmem_alloc(holder, 32);
@@ -203,43 +212,40 @@ __global__ void __launch_bounds__(128) fno_rowdft_kernel(const bf16* __restrict_
     const uint32_t tmem = *holder;
     const uint32_t idesc = U::idesc_bf16(128, NJ);
     const long long ntiles = rows / 128;
-    uint32_t phase = 0;
-    // The A tile goes straight from global to shared memory with cp.async, all
-    // of a thread's 16-byte pieces in flight at once; the next tile's copies
-    // are issued as soon as the MMAs have read the current one, under the
-    // epilogue.  8 consecutive threads fill one core matrix (8 rows x 16 B); a
-    // warp reads 64 contiguous bytes from each of 8 rows.
+    uint32_t phase = 0, tphase = 0;
+    // thread 0: the copies of tile t, issued as soon as the MMAs have read the
+    // previous tile, so they land under its epilogue
     auto stage = [&](long long t) {
-        const bf16* src = in + t * 128 * (long long)S;
-        for (int q = tid; q < 128 * KG; q += 128) {
-            const int r8 = q & 7, kg = (q >> 3) % KG, rg = (q >> 3) / KG;
-            U::cp_async16(sA + (rg * KG + kg) * 128 + r8 * 16, src + (size_t)(rg * 8 + r8) * S + kg * 8);
-        }
-        U::cp_async_commit();
+        U::mbar_arrive_expect_tx(tbar, A_BYTES);
+        for (int kg = 0; kg < KG; ++kg) U::tma_load_2d(sA + kg * KG_BYTES, &amap, kg * 8, (int)(t * 128), tbar);
     };
-    if ((long long)blockIdx.x < ntiles) stage(blockIdx.x);
+    if (tid == 0 && (long long)blockIdx.x < ntiles) stage(blockIdx.x);
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        U::cp_async_wait_all();
-        U::fence_proxy_async();
-        __syncthreads();
         if (tid == 0) {
-            U::fence_after();
-            const uint32_t a0 = U::smem_u32(sA), b0 = U::smem_u32(sB);
-#pragma unroll 4
-            for (int kk = 0; kk < S / 16; ++kk)
-                U::mma_bf16(tmem, U::desc(a0 + kk * 256, 128, KG * 128), U::desc(b0 + kk * 256, 128, KG * 128), idesc,
-                            kk > 0);
-            U::mma_commit(bar);
-            if (!U::mbar_wait(bar, phase)) {
+            if (!U::mbar_wait(tbar, tphase)) {
                 flag_error(err);
-                U::mbar_wait(bar, phase);
+                U::mbar_wait(tbar, tphase);
                 *abort_flag = 1;
+            } else {
+                U::fence_after();
+                const uint32_t a0 = U::smem_u32(sA), b0 = U::smem_u32(sB);
+#pragma unroll 4
+                for (int kk = 0; kk < S / 16; ++kk)
+                    U::mma_bf16(tmem, U::desc(a0 + kk * 2 * KG_BYTES, KG_BYTES, 128),
+                                U::desc(b0 + kk * 256, 128, KG * 128), idesc, kk > 0);
+                U::mma_commit(bar);
+                if (!U::mbar_wait(bar, phase)) {
+                    flag_error(err);
+                    U::mbar_wait(bar, phase);
+                    *abort_flag = 1;
+                }
             }
         }
         phase ^= 1u;
+        tphase ^= 1u;
         __syncthreads();
         if (*abort_flag) break;
-        if (t + gridDim.x < ntiles) stage(t + gridDim.x);  // the MMAs are done with sA
+        if (tid == 0 && t + gridDim.x < ntiles) stage(t + gridDim.x);  // the MMAs are done with sA
         U::fence_after();
         float v[32];
         U::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), v);
@@ -249,7 +255,6 @@ __global__ void __launch_bounds__(128) fno_rowdft_kernel(const bf16* __restrict_
         U::fence_before();
         __syncthreads();
     }
-    U::cp_async_wait_all();  // nothing left in flight (an aborted loop can leave a stage)
     __syncthreads();
     if (warp == 0) U::tmem_dealloc(tmem, 32);
 }
@@ -989,14 +994,54 @@ int grid_for(long long work, int per_sm)
     return (int)(work < g ? (work > 0 ? work : 1) : g);
 }
 
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+// (no link against the driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled()
+{
+    static const EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return EncodeTiledFn{nullptr};
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
 template <int S>
 int launch_rowdft(const bf16* in, long long rows, const void* mpack, float* out, int* err, cudaStream_t st)
 {
     constexpr int smem = 128 * S * 2 + NJ * S * 2 + 64;
+    // the tensor map: rows of S bf16 (S * 2 bytes apart), boxes of 8 columns x 128 rows
+    if ((reinterpret_cast<uintptr_t>(in) & 15) != 0 || rows % 128 != 0 || rows > 0x7fffffffLL)
+        return tt::invalid("fno_rowdft: rows must be 16-byte aligned, a multiple of 128 and below 2^31");
+    const EncodeTiledFn enc = encode_tiled();
+    if (!enc) {
+        tt::set_detail("fno_rowdft: cuTensorMapEncodeTiled is not available from the driver");
+        return TT_ERR_CUDA;
+    }
+    CUtensorMap map;
+    const cuuint64_t dims[2] = {(cuuint64_t)S, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)S * 2};
+    const cuuint32_t box[2] = {8, 128};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(in), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        tt::set_detail("fno_rowdft: cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return TT_ERR_CUDA;
+    }
     TT_TRY(tt::cuda_status(cudaFuncSetAttribute(fno_rowdft_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 smem),
                            "fno_rowdft attribute"));
-    fno_rowdft_kernel<S><<<grid_for(rows / 128, 2), 128, smem, st>>>(in, rows, (const uint4*)mpack, out, err);
+    fno_rowdft_kernel<S><<<grid_for(rows / 128, 2), 128, smem, st>>>(map, rows, (const uint4*)mpack, out, err);
     return tt::launch_status("fno_rowdft_kernel");
 }
 

@@ -121,6 +121,25 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
     return true;
 }
 
+// The next phase of *bar completes when this thread has arrived and `bytes`
+// bytes of asynchronous copies have landed (the barrier counts one arrival).
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// TMA: the box at coordinates (c0, c1) of the 2-D tensor map *map into shared
+// memory at dst (128-byte aligned), completing on *bar.  c0 * element size must
+// be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* map, int c0, int c1, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // 16-byte global -> shared copy (cp.async, L2 only); both addresses 16-byte aligned.
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
 {

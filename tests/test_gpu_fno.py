@@ -30,12 +30,13 @@ def _rel(a, b):
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(np.asarray(b)), 1e-300))
 
 
-@pytest.mark.parametrize("S", [128, 256])
-def test_rowdft_matches_float64(cuda, S):
+@pytest.mark.parametrize("S,rows", [(128, 384), (256, 384), (256, 128 * 700)])
+def test_rowdft_matches_float64(cuda, S, rows):
+    """Few tiles, and more 128-row tiles than the grid's blocks (each block
+    then loads its next tile while it finishes the current one)."""
     from turbulence_tracing_gb300 import fno
 
-    g = torch.Generator(device="cuda").manual_seed(S)
-    rows = 384
+    g = torch.Generator(device="cuda").manual_seed(S + rows)
     x = _bf(torch.randn((rows, S), device="cuda", generator=g))
     FxT, G = O.dft_mats(S)
     for M in (FxT, G * S * S):

@@ -12,9 +12,9 @@
 //                                                        DFT, fused, with a bias + GELU or
 //                                                        a GELU' epilogue
 //   wgrad   dW[o, c] += sum_p dz[o, p] v[c, p]           1x1 weight gradient
-// rowdft's input tiles arrive by TMA (cp.async.bulk.tensor); mix stages its
-// operands through registers (a transpose to K-major) and wgrad through
-// cp.async.  The DFT along y over the 32 retained ky (and its inverse), and the per-mode
+// rowdft's input tiles arrive by TMA (cp.async.bulk.tensor); mix and wgrad
+// stage their operands through registers (mix transposes to K-major on the
+// way).  The DFT along y over the 32 retained ky (and its inverse), and the per-mode
 // complex channel mixing, are small and run on the FP32 pipes.  The oracle's
 // restatement of the whole network is oracle/fno.py.
 //

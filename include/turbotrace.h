@@ -325,6 +325,26 @@ int tt_shadowgram(const float* theta, int P, double pitch, double D, float* inte
 int tt_shadowgram_batched(const float* theta, int nmaps, int P, double pitch, const double* D, float* intensity,
                           void* stream);
 
+/* The surrogate's network input from n march outputs maps FP32 [n][5][P][P]
+ * (tt_march_maps layout).  stats FP32 [n][4] (16-byte aligned) = (s, mean and
+ * unbiased standard deviation of the marched phase, log10(s (P - 1))), s the
+ * rms of the straight-line deflection; FP32 sums per thread, FP64 across
+ * them.  X FP32 [n][6][P][P] = (straight x, y, marched x, y) / s,
+ * (phase - mean) / sd, log10(s (P - 1)).  The learned surrogate has no
+ * counterpart in the reference. */
+int tt_surrogate_encode(const float* maps, int n, int P, float* X, float* stats, void* stream);
+/* theta FP32 [n][2][P][P] = maps[:, 0:2] + s / gain[0:2] * net[:, 0:2] (net
+ * FP32 [n][3][P][P] the network output, stats from tt_surrogate_encode, gain
+ * FP32 [3] the per-channel target gain), and theta_march FP32 [n][2][P][P] =
+ * maps[:, 0:2] when not NULL. */
+int tt_surrogate_decode(const float* maps, const float* net, const float* stats, const float* gain, int n, int P,
+                        float* theta, float* theta_march, void* stream);
+/* The fallback's error estimate: est FP32 [n] = kappa ||I_net - I_march|| /
+ * ||I_net|| over each P x P intensity map (FP32 sums per thread, FP64 across
+ * them; infinite when I_net is zero, so such a map falls back). */
+int tt_surrogate_estimate(const float* I_net, const float* I_march, int n, int P, double kappa, float* est,
+                          void* stream);
+
 /* ---- Learned surrogate: 2D Fourier neural operator ----------------------------
  * No reference interface: the reference has no surrogate.  The network maps
  * straight-line path-integrated gradient maps to the full-trace deflection and

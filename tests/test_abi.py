@@ -118,6 +118,10 @@ def test_march_and_shadowgram_arguments_checked_before_any_launch():
                                          8, fake, fake, need, None), b"fields"),
         (lambda: L.tt_march_maps_batched((ctypes.c_void_p * 33)(*([fake] * 33)), 33, _lib.TT_F32, 8, 8, 8, xp, xp, xp,
                                          1e-6, 1.0, 8, fake, fake, 33 * need, None), b"fields"),
+        (lambda: L.tt_surrogate_encode(fake, 0, 8, fake, fake, None), b"bad arguments"),
+        (lambda: L.tt_surrogate_encode(fake, 1, 8, fake, ctypes.c_void_p(0x1004), None), b"aligned"),
+        (lambda: L.tt_surrogate_decode(fake, fake, fake, None, 1, 8, fake, None, None), b"bad arguments"),
+        (lambda: L.tt_surrogate_estimate(fake, fake, 1, 8, -1.0, fake, None), b"bad arguments"),
         (lambda: L.tt_shadowgram_batched(fake, 0, 8, 1e-5, fake, fake, None), b"bad arguments"),
         (lambda: L.tt_shadowgram_batched(fake, 2, 1, 1e-5, fake, fake, None), b"bad arguments"),
         (lambda: L.tt_shadowgram_batched(fake, 2, 8, 0.0, fake, fake, None), b"bad arguments"),

@@ -201,6 +201,50 @@ def test_march_batched_equals_single_fields(cuda):
             assert torch.equal(b[i], core.march_maps(f, x, x, x, P, lwl=1064e-9)), (P, i)
 
 
+def test_surrogate_encode_decode_estimate_match_restatement(cuda):
+    """The fused input encoding, decoding and error estimate against float64
+    torch restatements; a zero network intensity gives an infinite estimate
+    (that map falls back)."""
+    from turbulence_tracing_gb300 import core
+    from turbulence_tracing_gb300 import surrogate as SG
+
+    g = torch.Generator(device="cuda").manual_seed(5)
+    n, P = 3, 96
+    amp = torch.tensor([1e-3, 2e-3, 5.0, 1e-3, 3e-3], device="cuda")
+    mm = torch.randn((n, 5, P, P), device="cuda", generator=g) * amp[None, :, None, None]
+    mm[:, 2] += 40.0  # a phase far from zero mean
+    X, st = core.surrogate_encode(mm)
+    m = mm.double()
+    s = torch.sqrt((m[:, 3:5] ** 2).mean(dim=(1, 2, 3)))
+    sd, mu = torch.std_mean(m[:, 2], dim=(1, 2))
+    ref = torch.empty((n, 6, P, P), dtype=torch.float64, device="cuda")
+    ref[:, 0:2] = m[:, 3:5] / s[:, None, None, None]
+    ref[:, 2:4] = m[:, 0:2] / s[:, None, None, None]
+    ref[:, 4] = (m[:, 2] - mu[:, None, None]) / sd[:, None, None]
+    ref[:, 5] = torch.log10(s * (P - 1))[:, None, None]
+    assert torch.allclose(st[:, 0].double(), s, rtol=1e-6, atol=0)
+    assert torch.allclose(st[:, 1].double(), mu, rtol=1e-6, atol=0)
+    assert torch.allclose(st[:, 2].double(), sd, rtol=1e-5, atol=0)
+    for c in range(6):
+        assert (X[:, c].double() - ref[:, c]).abs().max() <= 1e-5 * ref[:, c].abs().max(), c
+    X2 = torch.empty_like(X)
+    assert torch.equal(SG.encode_batch(mm, P, X2), st[:, 0]) and torch.equal(X2, X)
+    net = torch.randn((n, 3, P, P), device="cuda", generator=g)
+    gain = torch.tensor([700.0, 650.0, 40.0], device="cuda")
+    thm = torch.full((n, 2, P, P), float("nan"), device="cuda")
+    th = core.surrogate_decode(mm, net, st, gain, theta_march=thm)
+    th_ref = m[:, 0:2] + (st[:, 0].double()[:, None] / gain[0:2].double()[None, :])[:, :, None, None] * net[:, 0:2]
+    assert (th.double() - th_ref).abs().max() <= 1e-6 * th_ref.abs().max()
+    assert torch.equal(thm, mm[:, 0:2])
+    I_n = torch.rand((n, P, P), device="cuda", generator=g) + 0.5
+    I_m = I_n + 1e-3 * torch.randn((n, P, P), device="cuda", generator=g)
+    I_n[2] = 0.0
+    est = core.surrogate_estimate(I_n, I_m, 17.0)
+    ref_est = 17.0 * torch.linalg.norm((I_n - I_m).double(), dim=(1, 2)) / torch.linalg.norm(I_n.double(), dim=(1, 2))
+    assert torch.allclose(est[:2].double(), ref_est[:2], rtol=1e-6, atol=0)
+    assert torch.isinf(est[2])
+
+
 def test_march_is_close_to_exact_trace(cuda):
     """One field sample per cell and second order in z: on a field whose rays
     drift by cells the marched shadowgram is within 2% of the exact trace's,

@@ -131,6 +131,10 @@ SIGNATURES = {
                               ctypes.c_double, ctypes.c_double, c_int, c_void_p, c_void_p, c_size, c_void_p]),
     "tt_shadowgram": (c_int, [c_void_p, c_int, ctypes.c_double, ctypes.c_double, c_void_p, c_void_p, c_void_p]),
     "tt_shadowgram_batched": (c_int, [c_void_p, c_int, c_int, ctypes.c_double, c_void_p, c_void_p, c_void_p]),
+    "tt_surrogate_encode": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "tt_surrogate_decode": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p,
+                                    c_void_p]),
+    "tt_surrogate_estimate": (c_int, [c_void_p, c_void_p, c_int, c_int, ctypes.c_double, c_void_p, c_void_p]),
     "tt_fno_param_count": (c_size, [ctypes.POINTER(TTFnoDims)]),
     "tt_fno_workspace_bytes": (c_size, [ctypes.POINTER(TTFnoDims), c_int]),
     "tt_fno_forward": (c_int, [ctypes.POINTER(TTFnoDims), c_void_p, c_void_p, c_void_p, c_void_p, c_size, c_void_p]),

@@ -427,6 +427,53 @@ def shadowgram_batched(theta, pitch, D, intensity=None):
     return intensity
 
 
+def _f32_maps(t, nch, name):
+    if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and t.dim() == 4 and t.shape[1] == nch
+            and t.shape[2] == t.shape[3]):
+        raise ValueError("%s must be a contiguous float32 CUDA tensor (n, %d, P, P)" % (name, nch))
+
+
+def surrogate_encode(maps, X=None, stats=None):
+    """Network input X (n, 6, P, P) and stats (n, 4) = (s, phase mean, phase
+    sd, log10(s (P - 1))) from march outputs maps (n, 5, P, P)
+    (tt_surrogate_encode)."""
+    dev = require_cuda()
+    _f32_maps(maps, 5, "maps")
+    n, P = maps.shape[0], maps.shape[-1]
+    if X is None:
+        X = torch.empty((n, 6, P, P), dtype=torch.float32, device=dev)
+    if stats is None:
+        stats = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    _f32_maps(X, 6, "X")
+    check(_lib.lib().tt_surrogate_encode(_ptr(maps), n, P, _ptr(X), _ptr(stats), _stream()), "tt_surrogate_encode")
+    return X, stats
+
+
+def surrogate_decode(maps, net_out, stats, gain, theta=None, theta_march=None):
+    """theta (n, 2, P, P) = marched deflection + s / gain * network output, and
+    optionally the marched deflection into theta_march (tt_surrogate_decode)."""
+    dev = require_cuda()
+    _f32_maps(maps, 5, "maps")
+    _f32_maps(net_out, 3, "net_out")
+    n, P = maps.shape[0], maps.shape[-1]
+    if theta is None:
+        theta = torch.empty((n, 2, P, P), dtype=torch.float32, device=dev)
+    check(_lib.lib().tt_surrogate_decode(_ptr(maps), _ptr(net_out), _ptr(stats), _ptr(gain), n, P, _ptr(theta),
+                                         _ptr(theta_march), _stream()), "tt_surrogate_decode")
+    return theta
+
+
+def surrogate_estimate(I_net, I_march, kappa, est=None):
+    """est (n,) = kappa ||I_net - I_march|| / ||I_net|| per map (tt_surrogate_estimate)."""
+    dev = require_cuda()
+    n, P = I_net.shape[0], I_net.shape[-1]
+    if est is None:
+        est = torch.empty(n, dtype=torch.float32, device=dev)
+    check(_lib.lib().tt_surrogate_estimate(_ptr(I_net), _ptr(I_march), n, P, float(kappa), _ptr(est), _stream()),
+          "tt_surrogate_estimate")
+    return est
+
+
 def grf_field(n, L_box, alpha, ne0, delta, seed, dtype=torch.float32, kmin=None, kmax=None):
     """Band-limited unit-variance GRF density ne0 (1 + delta g) clipped >= 0, (n, n, n)."""
     dev = require_cuda()

@@ -883,3 +883,161 @@ extern "C" int tt_shadowgram_batched(const float* theta, int nmaps, int P, doubl
                                                                                     0.f, D, intensity, nullptr);
     return tt::launch_status("shadowgram_batched");
 }
+
+// ----------------------------------------------------------------------------- surrogate input and output
+// The network's input encoding and the fallback's error estimate, fused.  The
+// learned surrogate has no counterpart in the reference.
+namespace {
+
+// Block sums of three doubles in a fixed order (warp shuffles, then warp 0
+// over the warps' partials); the result is valid in thread 0.
+__device__ __forceinline__ void block_sum3(double& a, double& b, double& c)
+{
+    __shared__ double red[3][32];
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        b += __shfl_xor_sync(0xffffffffu, b, off);
+        c += __shfl_xor_sync(0xffffffffu, c, off);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) red[0][warp] = a, red[1][warp] = b, red[2][warp] = c;
+    __syncthreads();
+    if (warp == 0) {
+        a = lane < nw ? red[0][lane] : 0.0;
+        b = lane < nw ? red[1][lane] : 0.0;
+        c = lane < nw ? red[2][lane] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, off);
+            b += __shfl_xor_sync(0xffffffffu, b, off);
+            c += __shfl_xor_sync(0xffffffffu, c, off);
+        }
+    }
+}
+
+constexpr int kSurStatThreads = 1024;
+
+// One block per field: s = rms of the straight-line deflection (planes 3, 4),
+// the marched phase's mean and unbiased standard deviation (plane 2).  Each
+// thread sums its pixels in FP32 (the phase shifted by the field's first
+// value, so the variance does not cancel), the block adds the threads' sums
+// in FP64.
+__global__ void __launch_bounds__(kSurStatThreads) sur_encode_stats_kernel(const float* __restrict__ maps, int P,
+                                                                           float* __restrict__ stats)
+{
+    const size_t N = (size_t)P * P;
+    const float* __restrict__ m = maps + (size_t)blockIdx.x * 5 * N;
+    const float ref = m[2 * N];
+    float a = 0.f, b = 0.f, c = 0.f;
+    for (size_t p = threadIdx.x; p < N; p += kSurStatThreads) {
+        const float sx = m[3 * N + p], sy = m[4 * N + p], d = m[2 * N + p] - ref;
+        a = fmaf(sx, sx, fmaf(sy, sy, a));
+        b += d;
+        c = fmaf(d, d, c);
+    }
+    double A = a, B = b, C = c;
+    block_sum3(A, B, C);
+    if (threadIdx.x == 0) {
+        const float s = fmaxf((float)sqrt(A / (2.0 * (double)N)), 1e-30f);
+        const double md = B / (double)N;
+        const double var = fmax((C - B * md) / (double)(N - 1), 0.0);
+        float* st = stats + 4 * (size_t)blockIdx.x;
+        st[0] = s;
+        st[1] = (float)((double)ref + md);
+        st[2] = fmaxf((float)sqrt(var), 1e-30f);
+        st[3] = log10f(s * (float)(P - 1));
+    }
+}
+
+// X[f] = (straight x, y, marched x, y) / s, (phase - mean) / sd, log10(s (P - 1)).
+__global__ void sur_encode_write_kernel(const float* __restrict__ maps, int P, const float* __restrict__ stats,
+                                        float* __restrict__ X)
+{
+    const size_t N = (size_t)P * P;
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= N) return;
+    const float* __restrict__ m = maps + (size_t)blockIdx.y * 5 * N;
+    float* __restrict__ x = X + (size_t)blockIdx.y * 6 * N;
+    const float4 st = reinterpret_cast<const float4*>(stats)[blockIdx.y];
+    x[p] = m[3 * N + p] / st.x;
+    x[N + p] = m[4 * N + p] / st.x;
+    x[2 * N + p] = m[p] / st.x;
+    x[3 * N + p] = m[N + p] / st.x;
+    x[4 * N + p] = (m[2 * N + p] - st.y) / st.z;
+    x[5 * N + p] = st.w;
+}
+
+// theta = marched deflection + s / gain * network output (planes 0, 1), and
+// the marched deflection alone when theta_march is given.
+__global__ void sur_decode_kernel(const float* __restrict__ maps, const float* __restrict__ net,
+                                  const float* __restrict__ stats, const float* __restrict__ gain, int P,
+                                  float* __restrict__ theta, float* __restrict__ theta_march)
+{
+    const size_t N = (size_t)P * P;
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= N) return;
+    const size_t f = blockIdx.y;
+    const float s = stats[4 * f];
+    const float* __restrict__ m = maps + f * 5 * N;
+    const float* __restrict__ o = net + f * 3 * N;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        const float mv = m[c * N + p];
+        theta[(f * 2 + c) * N + p] = fmaf(s / gain[c], o[c * N + p], mv);
+        if (theta_march) theta_march[(f * 2 + c) * N + p] = mv;
+    }
+}
+
+// est[f] = kappa ||I_net - I_march|| / ||I_net|| (infinite when I_net is zero);
+// FP32 sums per thread, FP64 across the block.
+__global__ void __launch_bounds__(kSurStatThreads) sur_estimate_kernel(const float* __restrict__ In,
+                                                                       const float* __restrict__ Im, int P,
+                                                                       double kappa, float* __restrict__ est)
+{
+    const size_t N = (size_t)P * P;
+    const float* __restrict__ a_ = In + (size_t)blockIdx.x * N;
+    const float* __restrict__ b_ = Im + (size_t)blockIdx.x * N;
+    float a = 0.f, b = 0.f;
+    for (size_t p = threadIdx.x; p < N; p += kSurStatThreads) {
+        const float x = a_[p], d = x - b_[p];
+        a = fmaf(d, d, a);
+        b = fmaf(x, x, b);
+    }
+    double A = a, B = b, C = 0.0;
+    block_sum3(A, B, C);
+    if (threadIdx.x == 0) est[blockIdx.x] = B > 0.0 ? (float)(kappa * sqrt(A / B)) : __int_as_float(0x7f800000);
+}
+
+}  // namespace
+
+extern "C" int tt_surrogate_encode(const float* maps, int n, int P, float* X, float* stats, void* stream)
+{
+    if (!maps || !X || !stats || n < 1 || n > 65535 || P < 2 || P > 46340)
+        return tt::invalid("surrogate_encode: bad arguments");
+    if ((reinterpret_cast<uintptr_t>(stats) & 15) != 0) return tt::invalid("surrogate_encode: stats not 16-byte aligned");
+    cudaStream_t s = tt::as_stream(stream);
+    sur_encode_stats_kernel<<<n, kSurStatThreads, 0, s>>>(maps, P, stats);
+    TT_TRY(tt::launch_status("surrogate_encode stats"));
+    const size_t N = (size_t)P * P;
+    sur_encode_write_kernel<<<dim3((unsigned)((N + 255) / 256), n), 256, 0, s>>>(maps, P, stats, X);
+    return tt::launch_status("surrogate_encode");
+}
+
+extern "C" int tt_surrogate_decode(const float* maps, const float* net, const float* stats, const float* gain, int n,
+                                   int P, float* theta, float* theta_march, void* stream)
+{
+    if (!maps || !net || !stats || !gain || !theta || n < 1 || n > 65535 || P < 2 || P > 46340)
+        return tt::invalid("surrogate_decode: bad arguments");
+    const size_t N = (size_t)P * P;
+    sur_decode_kernel<<<dim3((unsigned)((N + 255) / 256), n), 256, 0, tt::as_stream(stream)>>>(
+        maps, net, stats, gain, P, theta, theta_march);
+    return tt::launch_status("surrogate_decode");
+}
+
+extern "C" int tt_surrogate_estimate(const float* I_net, const float* I_march, int n, int P, double kappa, float* est,
+                                     void* stream)
+{
+    if (!I_net || !I_march || !est || n < 1 || n > 65535 || P < 2 || P > 46340 || !(kappa >= 0))
+        return tt::invalid("surrogate_estimate: bad arguments");
+    sur_estimate_kernel<<<n, kSurStatThreads, 0, tt::as_stream(stream)>>>(I_net, I_march, P, kappa, est);
+    return tt::launch_status("surrogate_estimate");
+}

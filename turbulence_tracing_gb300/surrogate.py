@@ -121,17 +121,13 @@ class Workload:
 
 def encode_batch(mm, S, out):
     """Network inputs out (n, 6, S, S) and the scales s (n,) from march outputs
-    mm (n, 5, S, S): straight and marched deflections / s, the marched phase
-    standardised per field, log10 of the straight-line drift in cells."""
-    s = torch.sqrt((mm[:, 3:5] ** 2).mean(dim=(1, 2, 3))).clamp_min(1e-30)
-    sb = s[:, None, None, None]
-    out[:, 0:2] = mm[:, 3:5] / sb
-    out[:, 2:4] = mm[:, 0:2] / sb
-    ph = mm[:, 2]
-    sd, mu = torch.std_mean(ph, dim=(1, 2), keepdim=True)
-    out[:, 4] = (ph - mu) / sd.clamp_min(1e-30)
-    out[:, 5] = torch.log10(s * (S - 1))[:, None, None]
-    return s
+    mm (n, 5, S, S) on the device (tt_surrogate_encode): straight and marched
+    deflections / s (s the rms of the straight-line deflection), the marched
+    phase standardised per field, log10 of the straight-line drift in cells."""
+    if mm.shape[-1] != S:
+        raise ValueError("maps are %d^2, not %d^2" % (mm.shape[-1], S))
+    _, stats = core.surrogate_encode(mm, X=out)
+    return stats[:, 0]
 
 
 def encode(mm, S, k0, L, out=None):
@@ -315,6 +311,7 @@ class _Slot:
         self.D = torch.ones(batch, dtype=torch.float64, device=dev)
         self.D_host = torch.ones(batch, dtype=torch.float64).pin_memory()
         self.est = torch.empty(batch, dtype=torch.float32, device=dev)
+        self.stats = torch.empty((batch, 4), dtype=torch.float32, device=dev)
         self.est_host = torch.empty(batch, dtype=torch.float32).pin_memory()
         self.marched = torch.cuda.Event()  # the slot's maps are written
         self.ready = torch.cuda.Event()    # its estimates and kept intensities are out
@@ -356,15 +353,12 @@ class Pipeline:
 
     def _post(self, sl):
         W = self.W
-        s = encode_batch(sl.mar, W.S, sl.X)
+        core.surrogate_encode(sl.mar, X=sl.X, stats=sl.stats)
         self.net.forward(sl.X, out=sl.out)
-        torch.addcmul(sl.mar[:, 0:2], s[:, None, None, None] / W.gain[None, 0:2, None, None], sl.out[:, 0:2],
-                      out=sl.theta)
-        sl.theta_m.copy_(sl.mar[:, 0:2])
+        core.surrogate_decode(sl.mar, sl.out, sl.stats, W.gain, theta=sl.theta, theta_march=sl.theta_m)
         core.shadowgram_batched(sl.theta, W.pitch, sl.D, intensity=sl.I_n)
         core.shadowgram_batched(sl.theta_m, W.pitch, sl.D, intensity=sl.I_m)
-        torch.mul(torch.linalg.norm(sl.I_n - sl.I_m, dim=(1, 2)) / torch.linalg.norm(sl.I_n, dim=(1, 2)),
-                  self.kappa, out=sl.est)
+        core.surrogate_estimate(sl.I_n, sl.I_m, self.kappa, est=sl.est)
 
     def _launch(self, sl, chunk, D):
         """Queue a chunk: the slot is free (its previous chunk's results were
@@ -560,14 +554,14 @@ class TileScreen:
         """Returns (intensity (N, N), deflection (2, N, N), flagged tile indices)."""
         W, N, T = self.W, self.W.S, TILE
         mt = tile_maps(W.march(ne))
-        s = encode_batch(mt, T, self.X)
+        _, stats = core.surrogate_encode(mt, X=self.X)
         self.net.forward(self.X, out=self.out)
-        th = torch.addcmul(mt[:, 0:2], s[:, None, None, None] / W.gain[None, 0:2, None, None], self.out[:, 0:2])
+        thm = torch.empty((self.nt, 2, T, T), dtype=torch.float32, device=W.dev)
+        th = core.surrogate_decode(mt, self.out, stats, W.gain, theta_march=thm)
         Dv = torch.full((self.nt,), float(D), dtype=torch.float64, device=W.dev)
         I_n = core.shadowgram_batched(th, W.pitch, Dv)
-        I_m = core.shadowgram_batched(mt[:, 0:2].contiguous(), W.pitch, Dv)
-        est = (self.kappa * torch.linalg.norm((I_n - I_m).double(), dim=(1, 2)) /
-               torch.linalg.norm(I_n.double(), dim=(1, 2))).tolist()
+        I_m = core.shadowgram_batched(thm, W.pitch, Dv)
+        est = core.surrogate_estimate(I_n, I_m, self.kappa).tolist()
         flagged = [t for t in range(self.nt) if est[t] > self.tol]
         theta = untile(th, N).contiguous()
         if flagged:

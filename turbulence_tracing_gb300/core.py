@@ -433,6 +433,12 @@ def _f32_maps(t, nch, name):
         raise ValueError("%s must be a contiguous float32 CUDA tensor (n, %d, P, P)" % (name, nch))
 
 
+def _f32_dev(t, shape, name):
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()
+            and tuple(t.shape) == tuple(shape)):
+        raise ValueError("%s must be a contiguous float32 CUDA tensor of shape %s" % (name, tuple(shape)))
+
+
 def surrogate_encode(maps, X=None, stats=None):
     """Network input X (n, 6, P, P) and stats (n, 4) = (s, phase mean, phase
     sd, log10(s (P - 1))) from march outputs maps (n, 5, P, P)
@@ -445,6 +451,9 @@ def surrogate_encode(maps, X=None, stats=None):
     if stats is None:
         stats = torch.empty((n, 4), dtype=torch.float32, device=dev)
     _f32_maps(X, 6, "X")
+    _f32_dev(stats, (n, 4), "stats")
+    if X.shape[0] != n or X.shape[-1] != P:
+        raise ValueError("X must be (%d, 6, %d, %d)" % (n, P, P))
     check(_lib.lib().tt_surrogate_encode(_ptr(maps), n, P, _ptr(X), _ptr(stats), _stream()), "tt_surrogate_encode")
     return X, stats
 
@@ -456,8 +465,15 @@ def surrogate_decode(maps, net_out, stats, gain, theta=None, theta_march=None):
     _f32_maps(maps, 5, "maps")
     _f32_maps(net_out, 3, "net_out")
     n, P = maps.shape[0], maps.shape[-1]
+    if tuple(net_out.shape) != (n, 3, P, P):
+        raise ValueError("net_out must be (%d, 3, %d, %d)" % (n, P, P))
+    _f32_dev(stats, (n, 4), "stats")
+    _f32_dev(gain, (3,), "gain")
     if theta is None:
         theta = torch.empty((n, 2, P, P), dtype=torch.float32, device=dev)
+    _f32_dev(theta, (n, 2, P, P), "theta")
+    if theta_march is not None:
+        _f32_dev(theta_march, (n, 2, P, P), "theta_march")
     check(_lib.lib().tt_surrogate_decode(_ptr(maps), _ptr(net_out), _ptr(stats), _ptr(gain), n, P, _ptr(theta),
                                          _ptr(theta_march), _stream()), "tt_surrogate_decode")
     return theta
@@ -467,8 +483,11 @@ def surrogate_estimate(I_net, I_march, kappa, est=None):
     """est (n,) = kappa ||I_net - I_march|| / ||I_net|| per map (tt_surrogate_estimate)."""
     dev = require_cuda()
     n, P = I_net.shape[0], I_net.shape[-1]
+    _f32_dev(I_net, (n, P, P), "I_net")
+    _f32_dev(I_march, (n, P, P), "I_march")
     if est is None:
         est = torch.empty(n, dtype=torch.float32, device=dev)
+    _f32_dev(est, (n,), "est")
     check(_lib.lib().tt_surrogate_estimate(_ptr(I_net), _ptr(I_march), n, P, float(kappa), _ptr(est), _stream()),
           "tt_surrogate_estimate")
     return est

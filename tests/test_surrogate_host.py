@@ -20,8 +20,9 @@ def test_tiles_round_trip_and_pixel_indices():
 
 
 def test_encode_needs_the_gpu():
-    """The input encoding is a CUDA kernel (tt_surrogate_encode): without a GPU
-    it raises rather than computing on the host."""
+    """The input encoding, decoding and error estimate are CUDA kernels
+    (tt_surrogate_encode/decode/estimate): without a GPU they raise rather
+    than computing on the host."""
     import pytest
 
     if torch.cuda.is_available():
@@ -29,6 +30,12 @@ def test_encode_needs_the_gpu():
     mm = torch.zeros((1, 5, 8, 8))
     with pytest.raises(RuntimeError, match="CUDA"):
         SG.encode_batch(mm, 8, torch.empty((1, SG.IN_CHANNELS, 8, 8)))
+    from turbulence_tracing_gb300 import core
+
+    with pytest.raises(RuntimeError, match="CUDA"):
+        core.surrogate_decode(mm, torch.zeros((1, 3, 8, 8)), torch.zeros((1, 4)), torch.ones(3))
+    with pytest.raises(RuntimeError, match="CUDA"):
+        core.surrogate_estimate(torch.ones((1, 8, 8)), torch.ones((1, 8, 8)), 1.0)
 
 
 def test_targets_decode_round_trip():

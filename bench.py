@@ -81,6 +81,10 @@ def parse():
     ap.add_argument("--no-screen", action="store_true", help="skip the per-tile screening of the stress field")
     ap.add_argument("--screen-n", type=int, default=1024, help="stress-field grid for the tile screening leg")
     ap.add_argument("--screen-train", type=int, default=8, help="training fields (16 tiles each at 1024^3)")
+    ap.add_argument("--fp64-only", action="store_true",
+                    help="time only the plain FP64 drop-in on all --rays rays (--fp64-rtol/--fp64-atol)")
+    ap.add_argument("--fp64-rtol", type=float, default=1e-10)
+    ap.add_argument("--fp64-atol", type=float, default=1e-13)
     ap.add_argument("--json-out", default="")
     return ap.parse_args()
 
@@ -636,15 +640,16 @@ def screen_run(a):
 
 
 def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
-    """Public API: ElectronCube.solve(precision='fp32', phase=True) from pinned host
-    rays, then three ray_transfer_matrix diagnostics on the returned rays."""
+    """Public API, host buffers in and out, one new field per step: the
+    density (pinned host FP32) given to ElectronCube.external_ne, calc_dndr,
+    the pinned host rays as s0, solve(precision='fp32', phase=True) (the FP32
+    node volume is built from the uploaded density inside the step), then
+    three ray_transfer_matrix diagnostics on the returned numpy rays."""
     import torch
 
-    cube = pt.ElectronCube(x, x, x)
-    cube.external_ne(ne)
-    cube.calc_dndr(lwl=a.lwl)
-    cube.volume32()
+    ne_pinned = ne.cpu().pin_memory()
     pinned = torch.from_numpy(s0_host).pin_memory()
+    cube = pt.ElectronCube(x, x, x)
     bins_scale = 1
     import builtins
 
@@ -653,6 +658,8 @@ def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
     def one():
         builtins.print = lambda *k, **kw: None
         try:
+            cube.external_ne(ne_pinned)
+            cube.calc_dndr(lwl=a.lwl)
             cube.s0 = pinned
             rf = cube.solve(precision="fp32", phase=True)
         finally:
@@ -685,12 +692,12 @@ def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
     sec = float(np.median(times))
     units, sec = across_ranks(tot / k, sec, dist, dev)
     Np = s0_host.shape[1]
-    h2d = Np * 6 * 8 + 3 * Np * 4 * 8 + Np * 8          # s0; rf re-uploaded by each diagnostic; phase weights
+    h2d = ne.numel() * ne.element_size() + Np * 6 * 8   # density, s0 (the diagnostics use the rays' device twins)
     d2h = Np * (4 + 1) * 8 + Np * 2 * 4 + 4 * det * det * 8  # rf, phase; status, steps; 3 H + 1 Hw (sf stays on the device until read)
     return {"value": units / sec, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "seconds_per_step": sec, "steps": k, "step_seconds": times, "timing": "median step",
-            "path": "ElectronCube.solve(precision='fp32', phase=True) + Shadowgraphy, Schlieren_KE, "
-                    "phase-weighted Shadowgraphy histograms (numpy in, numpy out)"}
+            "path": "ElectronCube.external_ne(host density) + calc_dndr + solve(precision='fp32', phase=True) "
+                    "+ Shadowgraphy, Schlieren_KE, phase-weighted Shadowgraphy histograms (host arrays in and out)"}
 
 
 def _ref_path(a, dpath, td, rays, extra=()):
@@ -768,8 +775,41 @@ def run_reference(a):
             "detail": {"rays_per_s": rays_done / sec}}
 
 
+def run_fp64_only(a):
+    """The plain FP64 drop-in (tt_trace_f64, per-ray RK45, phase on) alone on
+    the workload's field and beam, every ray traced: one warm-up launch on a
+    small slice, then one launch over all rays timed with CUDA events."""
+    import torch
+
+    from oracle import restated as R
+    from turbulence_tracing_gb300 import core, turboGen
+
+    ne, x = turboGen.workload_field(a.n, a.L, a.alpha, a.delta, a.ne0, seed=a.seed, dtype=torch.float32)
+    ext = float(x.max())
+    s0 = torch.as_tensor(R.gaussian_beam(int(a.rays), a.sigma, a.div, ext, np.random.default_rng(a.seed)),
+                         device="cuda")
+    f = core.calc_dndr(ne, x, x, x, lwl=a.lwl)
+    t_end = R.t_end(ext)
+    core.trace_f64(f, s0[:, :1024], t_end, 2, ext, rtol=a.fp64_rtol, atol=a.fp64_atol, phase=True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    out = core.trace_f64(f, s0, t_end, 2, ext, rtol=a.fp64_rtol, atol=a.fp64_atol, phase=True)
+    e1.record()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    steps = int(out["nsteps"].sum().item())
+    return {"leg": "fp64_only", "grid": a.n, "rays": int(a.rays), "rtol": a.fp64_rtol, "atol": a.fp64_atol,
+            "seconds": sec, "rays_per_s": a.rays / sec, "ray_steps": steps, "ray_steps_per_s": steps / sec,
+            "steps_per_ray": steps / a.rays, "non_ok_rays": int((out["status"] != 0).sum().item())}
+
+
 def main():
     a = parse()
+    if a.fp64_only:
+        print(json.dumps(run_fp64_only(a)))
+        return
     res = run_ours(a) if a.impl == "ours" else run_reference(a)
     if res is not None:
         line = json.dumps(res)

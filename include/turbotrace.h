@@ -161,6 +161,40 @@ int tt_trace_f64(const double* dndx, const double* dndy, const double* dndz, con
                  double* sf, double* rf, double* phase, int32_t* status, int32_t* nsteps,
                  void* stream);
 
+/* An explicit Runge-Kutta pair in the form scipy.integrate's RungeKutta
+ * classes hold it (RK23, RK45, DOP853: class attributes A, B, C, E / E3, E5,
+ * error_estimator_order), for tt_trace_f64_rk -- the `method` argument of
+ * ElectronCube.solve, particle_tracker.py:312, 323.  n_stages s is 3, 6 or
+ * 12; A is strictly lower triangular with row sums C; B (s) sums to 1; E
+ * (s + 1 weights, the last on the FSAL evaluation at the new point) sums to 0.
+ * error_kind 0: err = h K^T E, RMS norm (RK23, RK45); error_kind 1 (12 stages
+ * only): DOP853's norm |h| |K^T E5|^2 / sqrt((|K^T E5|^2 + 0.01 |K^T E3|^2) n)
+ * with E5 in E and E3 in E3.  The step factor exponent is -1/(error_order+1),
+ * the initial-step exponent 1/(error_order+1). */
+#define TT_RK_MAX_STAGES 16
+typedef struct tt_rk_tableau {
+    int32_t n_stages;
+    int32_t error_order;
+    int32_t error_kind;
+    int32_t reserved;
+    double A[TT_RK_MAX_STAGES][TT_RK_MAX_STAGES];
+    double B[TT_RK_MAX_STAGES];
+    double C[TT_RK_MAX_STAGES];
+    double E[TT_RK_MAX_STAGES + 1];
+    double E3[TT_RK_MAX_STAGES + 1];
+} tt_rk_tableau;
+
+/* tt_trace_f64 with the caller's method: solve(method='RK23' | 'DOP853')
+ * (particle_tracker.py:312, 323 hands `method` to solve_ivp).  Same arguments
+ * and outputs as tt_trace_f64; tableau is a host struct. */
+int tt_trace_f64_rk(const double* dndx, const double* dndy, const double* dndz, const double* ne_nc,
+                    int nx, int ny, int nz, const double* x, const double* y, const double* z,
+                    double omega, const double* s0, int64_t np, double t_end,
+                    int probing_axis, double extent, const tt_trace_opts* opts,
+                    const tt_rk_tableau* tableau,
+                    double* sf, double* rf, double* phase, int32_t* status, int32_t* nsteps,
+                    void* stream);
+
 /* Persistent FP32 tracer over a tt_volume: rays binned by entry tile in the
  * volume's Morton order, one ray per thread pulled from a work queue, steps
  * ended on cell faces so each step integrates one cell's trilinear
@@ -418,6 +452,15 @@ int tt_fno_rowdft(int S, int64_t rows, const void* in, const void* mat_packed, f
 int tt_fno_mix(int S, int B, int mode, const void* in, const void* w_packed, const void* a_packed, const float* sp,
                const float* bias, const void* zprev, void* out0, void* out1, void* workspace, void* stream);
 int tt_fno_wgrad(int S, int B, const void* dz, const void* v, float* dW, float* db, void* workspace, void* stream);
+
+/* Test of the bounded-wait error path (no reference counterpart): tt_fno_rowdft
+ * with every mbarrier wait limited to wait_cycles SM clocks (1000..2e9) and
+ * the copies of each CTA's first tile left out, so that tile's barrier never
+ * completes.  Each CTA's wait runs out, it sets the error flag (workspace word
+ * 0, read with tt_fno_error_flag), frees its TMEM and returns; no copy is in
+ * flight when it does.  out is left unwritten. */
+int tt_fno_rowdft_timeout_test(int S, int64_t rows, const void* in, const void* mat_packed, float* out,
+                               void* workspace, int64_t wait_cycles, void* stream);
 
 #ifdef __cplusplus
 }

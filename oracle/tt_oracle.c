@@ -393,6 +393,185 @@ int tto_trace(const double* dndx, const double* dndy, const double* dndz,
 }
 
 /* ------------------------------------------------------------------------ */
+/* Any explicit Runge-Kutta pair of scipy.integrate's RungeKutta family
+ * (solve_ivp's method='RK23', 'RK45', 'DOP853'; particle_tracker.py:312, 323
+ * passes `method` through): scipy's rk_step (stages K[s] = f(y + h sum_j
+ * a[s][j] K[j]), y_new = y + h sum_j B[j] K[j], FSAL K[ns] = f(y_new)),
+ * _estimate_error_norm (RMS of h K^T E / scale; DOP853: |h| |e5|^2 /
+ * sqrt((|e5|^2 + 0.01 |e3|^2) n) with e = K^T E / scale), the step loop of
+ * _step_impl (factor 0.9 err^(-1/(q+1)) in [0.2, 10], min(1, .) after a
+ * rejection, TOO_SMALL below 10 spacings of t) and select_initial_step with
+ * the error order q.  Per ray, as integrate_ray. */
+typedef struct {
+    int ns, kind, order;
+    const double* A; /* ns x ns, row-major */
+    const double* B; /* ns */
+    const double* E; /* ns + 1 (E, or E5) */
+    const double* E3;/* ns + 1, kind 1 */
+} tto_rk;
+
+#define TTO_RK_MAX 16
+
+static double initial_step_q(const tto_cube* C, const double* y0, const double* f0,
+                             double t_bound, double rtol, double atol, int order, int64_t* nfev)
+{
+    const int n = C->neq;
+    double sc[7], tmp[7], y1[7], f1[7];
+    const double L = fabs(t_bound);
+    if (L == 0.0) return 0.0;
+    for (int i = 0; i < n; ++i) sc[i] = atol + fabs(y0[i]) * rtol;
+    for (int i = 0; i < n; ++i) tmp[i] = y0[i] / sc[i];
+    const double d0 = rms(tmp, n);
+    for (int i = 0; i < n; ++i) tmp[i] = f0[i] / sc[i];
+    const double d1 = rms(tmp, n);
+    double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
+    if (h0 > L) h0 = L;
+    for (int i = 0; i < n; ++i) y1[i] = y0[i] + h0 * f0[i];
+    rhs(C, y1, f1);
+    ++*nfev;
+    for (int i = 0; i < n; ++i) tmp[i] = (f1[i] - f0[i]) / sc[i];
+    const double d2 = rms(tmp, n) / h0;
+    double h1;
+    if (d1 <= 1e-15 && d2 <= 1e-15) {
+        h1 = h0 * 1e-3;
+        if (h1 < 1e-6) h1 = 1e-6;
+    } else {
+        const double m = d1 > d2 ? d1 : d2;
+        h1 = pow(0.01 / m, 1.0 / (order + 1));
+    }
+    double h = 100.0 * h0;
+    if (h1 < h) h = h1;
+    if (L < h) h = L;
+    return h;
+}
+
+static int integrate_ray_rk(const tto_cube* C, const tto_rk* T, double* y, double t_bound,
+                            double rtol, double atol, int64_t max_steps,
+                            int64_t* nacc, int64_t* nrej, int64_t* nfev)
+{
+    const int n = C->neq, ns = T->ns;
+    const double ex = -1.0 / (T->order + 1);
+    double f[7], K[TTO_RK_MAX + 1][7], yn[7], ys[7];
+    rhs(C, y, f);
+    *nfev = 1;
+    *nacc = 0;
+    *nrej = 0;
+    double h_abs = initial_step_q(C, y, f, t_bound, rtol, atol, T->order, nfev);
+    double t = 0.0;
+    if (t == t_bound) return TTO_OK;
+    for (;;) {
+        const double min_step = 10.0 * fabs(nextafter(t, INFINITY) - t);
+        if (h_abs < min_step) h_abs = min_step;
+        int rejected = 0;
+        double t_new, h;
+        for (;;) {
+            if (h_abs < min_step) return TTO_TOO_SMALL;
+            if (*nacc + *nrej >= max_steps) return TTO_MAXSTEPS;
+            h = h_abs;
+            t_new = t + h;
+            if (t_new - t_bound > 0) t_new = t_bound;
+            h = t_new - t;
+            h_abs = fabs(h);
+            for (int i = 0; i < n; ++i) K[0][i] = f[i];
+            for (int s = 1; s < ns; ++s) {
+                for (int i = 0; i < n; ++i) {
+                    double acc = 0.0;
+                    for (int j = 0; j < s; ++j) acc += K[j][i] * T->A[s * ns + j];
+                    ys[i] = y[i] + acc * h;
+                }
+                rhs(C, ys, K[s]);
+            }
+            for (int i = 0; i < n; ++i) {
+                double acc = 0.0;
+                for (int j = 0; j < ns; ++j) acc += K[j][i] * T->B[j];
+                yn[i] = y[i] + h * acc;
+            }
+            rhs(C, yn, K[ns]);
+            *nfev += ns;
+            double e5 = 0.0, e3 = 0.0;
+            for (int i = 0; i < n; ++i) {
+                const double ay = fabs(y[i]), an = fabs(yn[i]);
+                const double sc = atol + (ay > an ? ay : an) * rtol;
+                double a5 = 0.0, a3 = 0.0;
+                for (int j = 0; j <= ns; ++j) {
+                    a5 += K[j][i] * T->E[j];
+                    if (T->kind == 1) a3 += K[j][i] * T->E3[j];
+                }
+                if (T->kind == 1) {
+                    e5 += (a5 / sc) * (a5 / sc);
+                    e3 += (a3 / sc) * (a3 / sc);
+                } else {
+                    const double e = a5 * h / sc;
+                    e5 += e * e;
+                }
+            }
+            double en;
+            if (T->kind == 1)
+                en = (e5 == 0.0 && e3 == 0.0) ? 0.0 : fabs(h) * e5 / sqrt((e5 + 0.01 * e3) * n);
+            else
+                en = sqrt(e5) / sqrt((double)n);
+            if (en < 1.0) {
+                double factor;
+                if (en == 0.0) factor = 10.0;
+                else {
+                    factor = 0.9 * pow(en, ex);
+                    if (!(factor < 10.0)) factor = 10.0;
+                }
+                if (rejected && !(factor < 1.0)) factor = 1.0;
+                h_abs *= factor;
+                break;
+            } else {
+                double factor = 0.9 * pow(en, ex);
+                if (!(factor > 0.2)) factor = 0.2;
+                h_abs *= factor;
+                rejected = 1;
+                ++*nrej;
+            }
+        }
+        ++*nacc;
+        t = t_new;
+        for (int i = 0; i < n; ++i) { y[i] = yn[i]; f[i] = K[ns][i]; }
+        if (t - t_bound >= 0) return TTO_OK;
+    }
+}
+
+/* tto_trace with the method's tableau (ns <= 16 stages). */
+int tto_trace_rk(const double* dndx, const double* dndy, const double* dndz,
+                 const double* ne_nc, int nx, int ny, int nz,
+                 const double* x, const double* y, const double* z,
+                 double omega, const double* s0, int64_t np_total,
+                 int64_t first, int64_t count, double t_end,
+                 double rtol, double atol, int with_phase, int64_t max_steps,
+                 int ns, int kind, int order, const double* A, const double* B,
+                 const double* E, const double* E3,
+                 double* sf, double* phase, int64_t* nacc, int64_t* nrej,
+                 int64_t* nfev, int32_t* status)
+{
+    if (ns < 1 || ns > TTO_RK_MAX) return -1;
+    tto_cube C;
+    C.G.n[0] = nx; C.G.n[1] = ny; C.G.n[2] = nz;
+    C.G.g[0] = x; C.G.g[1] = y; C.G.g[2] = z;
+    C.dndx = dndx; C.dndy = dndy; C.dndz = dndz; C.ne_nc = ne_nc;
+    C.k0 = omega / TTO_C;
+    C.neq = with_phase ? 7 : 6;
+    tto_rk T = {ns, kind, order, A, B, E, E3};
+    for (int64_t r = first; r < first + count; ++r) {
+        double st[7];
+        for (int i = 0; i < 6; ++i) st[i] = s0[(size_t)i * np_total + r];
+        st[6] = 0.0;
+        int64_t a = 0, b = 0, c = 0;
+        const int code = integrate_ray_rk(&C, &T, st, t_end, rtol, atol, max_steps, &a, &b, &c);
+        for (int i = 0; i < 6; ++i) sf[(size_t)i * np_total + r] = st[i];
+        if (phase) phase[r] = with_phase ? st[6] : 0.0;
+        if (nacc) nacc[r] = a;
+        if (nrej) nrej[r] = b;
+        if (nfev) nfev[r] = c;
+        if (status) status[r] = code;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* numpy.histogram2d(x, y, bins=[nbx, nby], range=[[x0,x1],[y0,y1]]) followed by
  * the transpose at ray_transfer_matrix.py:188-191.  NaN samples are skipped
  * (the reference drops them at :185-186), samples outside the range are

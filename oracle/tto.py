@@ -41,6 +41,13 @@ def lib():
                                 ctypes.c_int64, ctypes.c_int64, ctypes.c_double,
                                 ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int64,
                                 _dp, _dp, _i64p, _i64p, _i64p, _i32p]
+        L.tto_trace_rk.restype = ctypes.c_int
+        L.tto_trace_rk.argtypes = [_dp, _dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   _dp, _dp, _dp, ctypes.c_double, _dp, ctypes.c_int64,
+                                   ctypes.c_int64, ctypes.c_int64, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int64,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp,
+                                   _dp, _dp, _i64p, _i64p, _i64p, _i32p]
         L.tto_histogram2d.restype = None
         L.tto_histogram2d.argtypes = [_dp, _dp, _dp, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -91,9 +98,27 @@ def default_threads():
         return os.cpu_count() or 1
 
 
+def rk_pair(method):
+    """(ns, kind, order, A, B, E, E3) of a scipy.integrate RungeKutta method
+    ('RK23', 'RK45', 'DOP853' or a RungeKutta subclass): the class attributes
+    solve_ivp itself integrates with."""
+    import scipy.integrate as si
+
+    cls = getattr(si, method) if isinstance(method, str) else method
+    ns = int(cls.n_stages)
+    a = np.asarray(cls.A, dtype=np.float64)
+    A = np.zeros((ns, ns))
+    A[:, :min(ns, a.shape[1])] = a[:ns, :ns]
+    B = _f64(np.asarray(cls.B)[:ns])
+    if hasattr(cls, "E5"):
+        return ns, 1, int(cls.error_estimator_order), A, B, _f64(cls.E5), _f64(cls.E3)
+    return ns, 0, int(cls.error_estimator_order), A, B, _f64(cls.E), _f64(np.zeros(ns + 1))
+
+
 def trace(dndx, dndy, dndz, x, y, z, s0, t_end, rtol=1e-10, atol=1e-12,
-          ne_nc=None, omega=None, max_steps=10_000_000, threads=None):
-    """Integrate every ray of s0 (6, Np) with its own RK45 instance.
+          ne_nc=None, omega=None, max_steps=10_000_000, threads=None, method=None):
+    """Integrate every ray of s0 (6, Np) with its own RK45 instance (or the
+    scipy RungeKutta method `method`, e.g. 'RK23', 'DOP853').
 
     Returns dict(sf=(6,Np), phase=(Np,) or None, nacc, nrej, nfev, status).
     Phase is integrated (as a 7th state) when ne_nc and omega are given.
@@ -115,13 +140,24 @@ def trace(dndx, dndy, dndz, x, y, z, s0, t_end, rtol=1e-10, atol=1e-12,
     threads = threads or default_threads()
     chunk = max(1, -(-Np // (threads * 4)))
 
+    rk = rk_pair(method) if method not in (None, "RK45") else None
+
     def run(first):
         cnt = min(chunk, Np - first)
-        L.tto_trace(_p(dndx), _p(dndy), _p(dndz), _p(ne_nc_a), nx, ny, nz,
-                    _p(x), _p(y), _p(z), float(omega or 0.0), _p(s0), Np, first, cnt,
-                    float(t_end), float(rtol), float(atol), int(with_phase), int(max_steps),
-                    _p(sf), _p(phase), _p(nacc, _i64p), _p(nrej, _i64p), _p(nfev, _i64p),
-                    _p(status, _i32p))
+        if rk is None:
+            L.tto_trace(_p(dndx), _p(dndy), _p(dndz), _p(ne_nc_a), nx, ny, nz,
+                        _p(x), _p(y), _p(z), float(omega or 0.0), _p(s0), Np, first, cnt,
+                        float(t_end), float(rtol), float(atol), int(with_phase), int(max_steps),
+                        _p(sf), _p(phase), _p(nacc, _i64p), _p(nrej, _i64p), _p(nfev, _i64p),
+                        _p(status, _i32p))
+        else:
+            ns, kind, order, A, B, E, E3 = rk
+            L.tto_trace_rk(_p(dndx), _p(dndy), _p(dndz), _p(ne_nc_a), nx, ny, nz,
+                           _p(x), _p(y), _p(z), float(omega or 0.0), _p(s0), Np, first, cnt,
+                           float(t_end), float(rtol), float(atol), int(with_phase), int(max_steps),
+                           ns, kind, order, _p(A), _p(B), _p(E), _p(E3),
+                           _p(sf), _p(phase), _p(nacc, _i64p), _p(nrej, _i64p), _p(nfev, _i64p),
+                           _p(status, _i32p))
 
     starts = list(range(0, Np, chunk))
     if threads == 1 or len(starts) == 1:

@@ -229,12 +229,17 @@ def test_analytic_densities_vs_oracle(cuda, name, kw):
 
 
 def test_over_critical_liner(cuda):
-    """test_liner at 2e27 m^-3 (the notebook's over-critical liner): ne/n_c is
-    clipped at ne_max = 1 and rays are turned back at the clip edge.  Every
-    ray finishes; FP64 is within the bars of the oracle on every ray, FP32 on
-    at least 98% of them (the rays turned back at the edge of the clipped
-    core, where the slowest point of the turn meets FP32's resolution, stay
-    within 1e-5 rad and 1e-5 L)."""
+    """test_liner at 2e27 m^-3 (the notebook's over-critical liner, clipped at
+    ne_max = 1, calc_dndr particle_tracker.py:230-232), FP32 at its default
+    tolerance and FP64, against the oracle converged far below the bars.
+
+    Truth: the oracle at rtol 1e-13, 3e-14 and 1e-14.  On this field a few
+    rays turned back at the clip edge are ill-conditioned: the oracle's own
+    answers at those tolerances differ by up to 2e-5 rad (and the rtol-1e-10
+    oracle by 3e-6 rad from them), so the 1 urad bar cannot tell a right
+    answer from a wrong one there.  Every ray must meet the bars against one
+    of the converged oracle answers, and every well-conditioned ray (the
+    oracle answers agree within 1e-7) against all of them."""
     from turbulence_tracing_gb300 import particle_tracker as pt
 
     x = np.linspace(-1e-3, 1e-3, 41)
@@ -242,16 +247,36 @@ def test_over_critical_liner(cuda):
     cube.test_liner(n_e0=2e27, LR=1e-3)
     cube.calc_dndr(lwl=LWL)
     s0 = R.gaussian_beam(200, 0.4e-3, 0.05e-3, x.max(), np.random.default_rng(4))
-    ref = oracle_trace(np.asarray(cube.ne), x, s0)
-    for prec, tol in (("fp32", {}), ("fp64", {"rtol": 1e-10, "atol": 1e-12})):
+    ne = np.asarray(cube.ne)
+    refs = [oracle_trace(ne, x, s0, rtol=rt, atol=at) for rt, at in ((1e-13, 1e-17), (3e-14, 1e-18), (1e-14, 1e-18))]
+    L2 = 2 * x.max()
+
+    def per_ray(rf, ph, r):
+        pos = np.abs(rf[0::2] - r["rf"][0::2]).max(axis=0) / L2
+        ang = np.abs(rf[1::2] - r["rf"][1::2]).max(axis=0)
+        return pos, ang, np.abs(ph - r["phase"])
+
+    spread = np.zeros(s0.shape[1])
+    for i in range(len(refs)):
+        for j in range(i):
+            p_, a_, _ = per_ray(refs[i]["rf"], refs[i]["phase"], refs[j])
+            spread = np.maximum(spread, np.maximum(p_, a_))
+    well = spread <= 1e-7
+    assert well.mean() >= 0.98, spread.max()
+    for prec, tol in (("fp32", {}), ("fp64", {"rtol": 1e-13, "atol": 1e-17})):
         cube.s0 = s0.copy()
         rf = np.asarray(cube.solve(precision=prec, phase=True, **tol))
+        ph = np.asarray(cube.phase)
         st = np.asarray(cube.status)
-        pos = np.abs(rf[0::2] - ref["rf"][0::2]).max(axis=0) / (2 * x.max())
-        ang = np.abs(rf[1::2] - ref["rf"][1::2]).max(axis=0)
-        ok = (pos <= POS_BAR) & (ang <= ANG_BAR)
         assert (st == 0).all() and np.isfinite(rf).all()
-        if prec == "fp64":
-            assert ok.all(), (pos.max(), ang.max())
-        else:
-            assert ok.mean() >= 0.98 and pos.max() <= 1e-5 and ang.max() <= 1e-5, (ok.mean(), pos.max(), ang.max())
+        ok_any = np.zeros(s0.shape[1], bool)
+        ok_all = np.ones(s0.shape[1], bool)
+        worst = 0.0
+        for r in refs:
+            pos, ang, dph = per_ray(rf, ph, r)
+            ok = (pos <= POS_BAR) & (ang <= ANG_BAR) & (dph <= PHASE_BAR)
+            ok_any |= ok
+            ok_all &= ok
+            worst = max(worst, float(np.max(np.where(well, np.maximum(pos, ang), 0.0))))
+        assert ok_any.all(), (prec, np.where(~ok_any)[0])
+        assert ok_all[well].all(), (prec, worst, np.where(well & ~ok_all)[0])

@@ -58,6 +58,16 @@ class TTTraceOpts(ctypes.Structure):
                 ("ray_chunk", ctypes.c_int32)]
 
 
+TT_RK_MAX_STAGES = 16
+
+
+class TTRKTableau(ctypes.Structure):
+    _fields_ = [("n_stages", ctypes.c_int32), ("error_order", ctypes.c_int32), ("error_kind", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("A", (ctypes.c_double * TT_RK_MAX_STAGES) * TT_RK_MAX_STAGES),
+                ("B", ctypes.c_double * TT_RK_MAX_STAGES), ("C", ctypes.c_double * TT_RK_MAX_STAGES),
+                ("E", ctypes.c_double * (TT_RK_MAX_STAGES + 1)), ("E3", ctypes.c_double * (TT_RK_MAX_STAGES + 1))]
+
+
 class TTFnoDims(ctypes.Structure):
     _fields_ = [("batch", ctypes.c_int32), ("size", ctypes.c_int32), ("in_ch", ctypes.c_int32),
                 ("out_ch", ctypes.c_int32), ("layers", ctypes.c_int32)]
@@ -96,6 +106,10 @@ SIGNATURES = {
                              c_void_p, ctypes.c_double, c_void_p, c_i64, ctypes.c_double, c_int,
                              ctypes.c_double, ctypes.POINTER(TTTraceOpts), c_void_p, c_void_p, c_void_p,
                              c_void_p, c_void_p, c_void_p]),
+    "tt_trace_f64_rk": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p,
+                                c_void_p, ctypes.c_double, c_void_p, c_i64, ctypes.c_double, c_int,
+                                ctypes.c_double, ctypes.POINTER(TTTraceOpts), ctypes.POINTER(TTRKTableau), c_void_p,
+                                c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tt_trace_f32_workspace_bytes": (c_size, [ctypes.POINTER(TTVolume), c_i64]),
     "tt_trace_f32": (c_int, [ctypes.POINTER(TTVolume), c_void_p, c_i64, ctypes.c_double, ctypes.c_double,
                              ctypes.POINTER(TTTraceOpts), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
@@ -150,6 +164,7 @@ SIGNATURES = {
     "tt_fno_mix": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                            c_void_p, c_void_p, c_void_p, c_void_p]),
     "tt_fno_wgrad": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tt_fno_rowdft_timeout_test": (c_int, [c_int, c_i64, c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
 }
 
 _lib = None

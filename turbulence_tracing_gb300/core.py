@@ -11,6 +11,7 @@ unavailable.
 """
 import ctypes
 import math
+import weakref
 
 import numpy as np
 import torch
@@ -38,6 +39,9 @@ def _ptr(t):
 def _f64_dev(a, dev):
     if isinstance(a, torch.Tensor):
         return a.to(device=dev, dtype=torch.float64).contiguous()
+    tw = device_twin(a)
+    if tw is not None and tw.device == dev and tw.dtype == torch.float64:
+        return tw
     return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=dev)
 
 
@@ -58,16 +62,54 @@ def _dtype_code(t):
     return _lib.TT_F32 if t.dtype == torch.float32 else _lib.TT_F64
 
 
-def to_host(t):
+# Device twins: host arrays returned with twin=True remember the device tensor
+# they were copied from, so handing the same array back to a library call
+# (e.g. ElectronCube.rf to a ray_transfer_matrix diagnostic) uses the device
+# copy instead of uploading it again.  Such arrays are returned read-only: an
+# in-place write needs arr.setflags(write=True) first, which ends the twin
+# (a writeable array is always uploaded afresh), so a twin never goes stale.
+_twins = {}
+
+
+def _forget(key):
+    _twins.pop(key, None)
+
+
+def to_host(t, twin=False):
     """Device tensor -> numpy array through a pinned staging buffer (torch's
     caching host allocator), so large results come back at the host link's
-    speed rather than through pageable copies.  Each call returns fresh memory."""
+    speed rather than through pageable copies.  Each call returns fresh memory.
+    twin=True: the array comes back read-only and keeps t as its device twin."""
     if t.numel() * t.element_size() < (1 << 20):
-        return t.cpu().numpy()
-    h = torch.empty(tuple(t.shape), dtype=t.dtype, device="cpu", pin_memory=True)
-    h.copy_(t, non_blocking=True)
-    torch.cuda.current_stream().synchronize()
-    return h.numpy()
+        a = t.cpu().numpy()
+    else:
+        h = torch.empty(tuple(t.shape), dtype=t.dtype, device="cpu", pin_memory=True)
+        h.copy_(t, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        a = h.numpy()
+    if twin:
+        a.flags.writeable = False
+        key = id(a)
+        _twins[key] = (weakref.ref(a, lambda _r, k=key: _forget(k)), t)
+    return a
+
+
+def device_twin(a):
+    """The device tensor a read-only array returned by to_host(twin=True) was
+    copied from, or None (not such an array, or made writeable since)."""
+    if not isinstance(a, np.ndarray):
+        return None
+    e = _twins.get(id(a))
+    if e is None or e[0]() is not a or a.flags.writeable:
+        return None
+    return e[1]
+
+
+def release_twin(a):
+    """Drop a's device twin and make a writeable again (for in-place writes)."""
+    if isinstance(a, np.ndarray) and id(a) in _twins and _twins[id(a)][0]() is a:
+        _forget(id(a))
+        a.flags.writeable = True
 
 
 def workspace(nbytes, dev):
@@ -191,10 +233,55 @@ def _ray_outputs(np_, dev, want_sf=True):
                 nsteps=torch.empty((np_,), dtype=torch.int32, device=dev))
 
 
-def trace_f64(fields, s0, t_end, probing_axis, extent, rtol=1e-3, atol=1e-6, phase=False, max_steps=None):
-    """Plain FP64 drop-in tracer.  fields: dict from calc_dndr.  s0: (6, Np)."""
+EXPLICIT_RK_METHODS = ("RK23", "RK45", "DOP853")
+
+
+def rk_tableau(method):
+    """tt_rk_tableau of an explicit Runge-Kutta method of scipy.integrate:
+    'RK23', 'RK45', 'DOP853' or a RungeKutta subclass (as solve_ivp's `method`
+    accepts).  The coefficients are the class attributes solve_ivp itself
+    integrates with (A, B, C, E, or E5/E3 for DOP853; error_estimator_order)."""
+    import scipy.integrate as si
+
+    cls = getattr(si, method, None) if isinstance(method, str) else method
+    if cls is None or not all(hasattr(cls, a) for a in ("A", "B", "C", "n_stages", "error_estimator_order")):
+        raise NotImplementedError(
+            "method %r: the GPU integrates solve_ivp's explicit Runge-Kutta methods (%s); the implicit "
+            "stiff solvers (Radau, BDF, LSODA) are not provided -- the ray equation is not stiff"
+            % (method, ", ".join(EXPLICIT_RK_METHODS)))
+    ns = int(cls.n_stages)
+    if ns not in (3, 6, 12):
+        raise NotImplementedError("method %r: %d stages; the GPU kernels take 3, 6 or 12" % (method, ns))
+    t = _lib.TTRKTableau()
+    t.n_stages = ns
+    t.error_order = int(cls.error_estimator_order)
+    A = np.asarray(cls.A, dtype=np.float64)
+    for i in range(ns):
+        for j in range(min(i, A.shape[1])):
+            t.A[i][j] = float(A[i, j])
+    for i in range(ns):
+        t.B[i] = float(np.asarray(cls.B, dtype=np.float64)[i])
+        t.C[i] = float(np.asarray(cls.C, dtype=np.float64)[i])
+    if hasattr(cls, "E5"):
+        t.error_kind = 1
+        for i in range(ns + 1):
+            t.E[i] = float(cls.E5[i])
+            t.E3[i] = float(cls.E3[i])
+    else:
+        t.error_kind = 0
+        for i in range(ns + 1):
+            t.E[i] = float(cls.E[i])
+    return t
+
+
+def trace_f64(fields, s0, t_end, probing_axis, extent, rtol=1e-3, atol=1e-6, phase=False, max_steps=None,
+              method="RK45"):
+    """Plain FP64 drop-in tracer.  fields: dict from calc_dndr.  s0: (6, Np).
+    method: solve_ivp's explicit Runge-Kutta methods ('RK45' built in; 'RK23',
+    'DOP853' or a scipy RungeKutta subclass through tt_trace_f64_rk)."""
     dev = require_cuda()
     L = _lib.lib()
+    tab = None if (isinstance(method, str) and method == "RK45") else rk_tableau(method)
     s0_t = _f64_dev(s0, dev)
     if s0_t.dim() != 2 or s0_t.shape[0] != 6:
         raise ValueError("s0 must be (6, Np)")
@@ -203,11 +290,15 @@ def trace_f64(fields, s0, t_end, probing_axis, extent, rtol=1e-3, atol=1e-6, pha
     nx, ny, nz = fields["dndx"].shape
     xs, ys, zs = fields["coords"]
     o = _opts(rtol, atol, 0.0, max_steps, phase)
-    check(L.tt_trace_f64(_ptr(fields["dndx"]), _ptr(fields["dndy"]), _ptr(fields["dndz"]), _ptr(fields["ne_nc"]),
-                         nx, ny, nz, _ptr(xs), _ptr(ys), _ptr(zs), float(fields["omega"]), _ptr(s0_t), np_,
-                         float(t_end), int(probing_axis), float(extent), ctypes.byref(o), _ptr(out["sf"]),
-                         _ptr(out["rf"]), _ptr(out["phase"]), _ptr(out["status"]), _ptr(out["nsteps"]),
-                         _stream()), "tt_trace_f64")
+    args = (_ptr(fields["dndx"]), _ptr(fields["dndy"]), _ptr(fields["dndz"]), _ptr(fields["ne_nc"]),
+            nx, ny, nz, _ptr(xs), _ptr(ys), _ptr(zs), float(fields["omega"]), _ptr(s0_t), np_,
+            float(t_end), int(probing_axis), float(extent), ctypes.byref(o))
+    outs = (_ptr(out["sf"]), _ptr(out["rf"]), _ptr(out["phase"]), _ptr(out["status"]), _ptr(out["nsteps"]),
+            _stream())
+    if tab is None:
+        check(L.tt_trace_f64(*args, *outs), "tt_trace_f64")
+    else:
+        check(L.tt_trace_f64_rk(*args, ctypes.byref(tab), *outs), "tt_trace_f64_rk")
     return out
 
 

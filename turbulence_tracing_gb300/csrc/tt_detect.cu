@@ -3,8 +3,10 @@
 // Replaces Rays.__init__ (m_to_mm), the diagnostics' solve() chains and
 // Rays.histogram of particle_tracking/ray_transfer_matrix.py:37-195, 214-299.
 // One thread carries one ray through the optic chain (4x4 transfer matrices
-// applied as numpy.matmul does, zero terms included so inf/NaN propagate the
-// same way; filters set every component of a rejected ray to NaN), then bins
+// applied as numpy.matmul does: the block-diagonal terms alone while the ray
+// is finite, which round identically, the full product with its zero terms
+// otherwise so inf/NaN propagate the same way; filters set every component
+// of a rejected ray to NaN), then bins
 // the survivors with numpy.histogram2d's rule: edges = linspace(lo, hi, n+1)
 // computed as numpy computes them, bin = searchsorted(edges, v, 'right') - 1,
 // the right edge belongs to the last bin, out-of-range and NaN dropped.
@@ -57,6 +59,19 @@ __device__ inline void set_nan(double r[4])
     r[0] = r[1] = r[2] = r[3] = CUDART_NAN;
 }
 
+// Every component finite (exponent field not all ones): then the zero terms
+// of a transfer matrix add exact zeros and its unit terms are exact, so the
+// block-diagonal products below round exactly as the full 4x4 product does
+// (up to the sign of a zero result); otherwise the full product runs so that
+// inf and NaN spread across components as numpy's matmul spreads them.
+__device__ inline bool all_finite(const double r[4])
+{
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ok = ok && (((unsigned)__double2hiint(r[k]) & 0x7ff00000u) != 0x7ff00000u);
+    return ok;
+}
+
 __device__ inline void apply_chain(const Chain& C, double r[4])
 {
     for (int k = 0; k < C.n; ++k) {
@@ -65,6 +80,11 @@ __device__ inline void apply_chain(const Chain& C, double r[4])
             case TT_OPTIC_DISTANCE: {
                 // [[1,d],[0,1]] blocks: out0 = 1 r0 + d r1 + 0 r2 + 0 r3, ...
                 const double d = o.p[0];
+                if (all_finite(r)) {
+                    r[0] = r[0] + d * r[1];
+                    r[2] = r[2] + d * r[3];
+                    break;
+                }
                 const double a0 = 1.0 * r[0] + d * r[1] + 0.0 * r[2] + 0.0 * r[3];
                 const double a1 = 0.0 * r[0] + 1.0 * r[1] + 0.0 * r[2] + 0.0 * r[3];
                 const double a2 = 0.0 * r[0] + 0.0 * r[1] + 1.0 * r[2] + d * r[3];
@@ -73,7 +93,12 @@ __device__ inline void apply_chain(const Chain& C, double r[4])
                 break;
             }
             case TT_OPTIC_LENS: {
-                const double m1 = -1.0 / o.p[0], m2 = -1.0 / o.p[1];
+                const double m1 = o.p[0], m2 = o.p[1];  // -1/f1, -1/f2, formed on the host
+                if (all_finite(r)) {
+                    r[1] = m1 * r[0] + r[1];
+                    r[3] = m2 * r[2] + r[3];
+                    break;
+                }
                 const double a0 = 1.0 * r[0] + 0.0 * r[1] + 0.0 * r[2] + 0.0 * r[3];
                 const double a1 = m1 * r[0] + 1.0 * r[1] + 0.0 * r[2] + 0.0 * r[3];
                 const double a2 = 0.0 * r[0] + 0.0 * r[1] + 1.0 * r[2] + 0.0 * r[3];
@@ -204,6 +229,10 @@ extern "C" int tt_detect(const double* rf, int64_t n, const tt_optic* chain_host
         if (kind < TT_OPTIC_DISTANCE || kind > TT_OPTIC_M_TO_MM) return tt::invalid("detect: unknown optic kind");
         if (kind == TT_OPTIC_KNIFE_EDGE && C.op[k].p[2] == 0.0)
             return tt::invalid("detect: knife edge direction must be < 0 or > 0");
+        if (kind == TT_OPTIC_LENS) {  // the matrix entries -1/f, rounded once as numpy rounds them
+            C.op[k].p[0] = -1.0 / C.op[k].p[0];
+            C.op[k].p[1] = -1.0 / C.op[k].p[1];
+        }
     }
     Axis AX{x0, x1, (x1 - x0) / (double)nbx, nbx};
     Axis AY{y0, y1, (y1 - y0) / (double)nby, nby};

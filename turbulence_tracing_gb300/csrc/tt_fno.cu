@@ -181,10 +181,15 @@ __global__ void fno_pack_weights_kernel(WPackArgs a, const float* __restrict__ p
 // 8 columns x 128 rows, and box kg lands at sA + kg * 2048 as 16 core matrices
 // (8 rows x 16 B) stacked along the rows.  So in the A descriptor the core
 // matrices adjacent along K are 2048 B apart and the 8-row groups 128 B.
+// wait_cycles bounds every mbarrier wait; skip_first_copy (tests only) leaves
+// out the copies of each CTA's first tile, so its tile barrier never completes
+// and the kernel takes its timeout path (error flag, TMEM freed, return) with
+// no copy in flight.
 template <int S>
 __global__ void __launch_bounds__(128) fno_rowdft_kernel(const __grid_constant__ CUtensorMap amap, long long rows,
                                                          const uint4* __restrict__ mpack, float* __restrict__ out,
-                                                         int* __restrict__ err)
+                                                         int* __restrict__ err, long long wait_cycles,
+                                                         int skip_first_copy)
 {
     namespace U = tt::umma;
     constexpr int KG = S / 8;
@@ -219,14 +224,15 @@ __global__ void __launch_bounds__(128) fno_rowdft_kernel(const __grid_constant__
     // previous tile, so they land under its epilogue
     auto stage = [&](long long t) {
         U::mbar_arrive_expect_tx(tbar, A_BYTES);
+        if (skip_first_copy && t == (long long)blockIdx.x) return;
         for (int kg = 0; kg < KG; ++kg) U::tma_load_2d(sA + kg * KG_BYTES, &amap, kg * 8, (int)(t * 128), tbar);
     };
     if (tid == 0 && (long long)blockIdx.x < ntiles) stage(blockIdx.x);
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         if (tid == 0) {
-            if (!U::mbar_wait(tbar, tphase)) {
+            if (!U::mbar_wait(tbar, tphase, wait_cycles)) {
                 flag_error(err);
-                U::mbar_wait(tbar, tphase);
+                U::mbar_wait(tbar, tphase, wait_cycles);
                 *abort_flag = 1;
             } else {
                 U::fence_after();
@@ -236,9 +242,9 @@ __global__ void __launch_bounds__(128) fno_rowdft_kernel(const __grid_constant__
                     U::mma_bf16(tmem, U::desc(a0 + kk * 2 * KG_BYTES, KG_BYTES, 128),
                                 U::desc(b0 + kk * 256, 128, KG * 128), idesc, kk > 0);
                 U::mma_commit(bar);
-                if (!U::mbar_wait(bar, phase)) {
+                if (!U::mbar_wait(bar, phase, wait_cycles)) {
                     flag_error(err);
-                    U::mbar_wait(bar, phase);
+                    U::mbar_wait(bar, phase, wait_cycles);
                     *abort_flag = 1;
                 }
             }
@@ -1017,7 +1023,8 @@ EncodeTiledFn encode_tiled()
 }
 
 template <int S>
-int launch_rowdft(const bf16* in, long long rows, const void* mpack, float* out, int* err, cudaStream_t st)
+int launch_rowdft(const bf16* in, long long rows, const void* mpack, float* out, int* err, cudaStream_t st,
+                  long long wait_cycles = tt::umma::kWaitCycles, int skip_first_copy = 0)
 {
     constexpr int smem = 128 * S * 2 + NJ * S * 2 + 64;
     // the tensor map: rows of S bf16 (S * 2 bytes apart), boxes of 8 columns x 128 rows
@@ -1043,7 +1050,8 @@ int launch_rowdft(const bf16* in, long long rows, const void* mpack, float* out,
     TT_TRY(tt::cuda_status(cudaFuncSetAttribute(fno_rowdft_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 smem),
                            "fno_rowdft attribute"));
-    fno_rowdft_kernel<S><<<grid_for(rows / 128, 2), 128, smem, st>>>(map, rows, (const uint4*)mpack, out, err);
+    fno_rowdft_kernel<S><<<grid_for(rows / 128, 2), 128, smem, st>>>(map, rows, (const uint4*)mpack, out, err,
+                                                                      wait_cycles, skip_first_copy);
     return tt::launch_status("fno_rowdft_kernel");
 }
 
@@ -1285,6 +1293,19 @@ int tt_fno_rowdft(int S, int64_t rows, const void* in, const void* mat_packed, f
     int* err = static_cast<int*>(ws);
     return S == 128 ? launch_rowdft<128>((const bf16*)in, rows, mat_packed, out, err, st)
                     : launch_rowdft<256>((const bf16*)in, rows, mat_packed, out, err, st);
+}
+
+int tt_fno_rowdft_timeout_test(int S, int64_t rows, const void* in, const void* mat_packed, float* out, void* ws,
+                               int64_t wait_cycles, void* stream)
+{
+    if ((S != 128 && S != 256) || rows <= 0 || rows % 128 || !in || !mat_packed || !out || !ws)
+        return tt::invalid("tt_fno_rowdft_timeout_test: bad arguments");
+    if (wait_cycles < 1000 || wait_cycles > tt::umma::kWaitCycles)
+        return tt::invalid("tt_fno_rowdft_timeout_test: wait_cycles must be in [1000, 2e9]");
+    cudaStream_t st = tt::as_stream(stream);
+    int* err = static_cast<int*>(ws);
+    return S == 128 ? launch_rowdft<128>((const bf16*)in, rows, mat_packed, out, err, st, wait_cycles, 1)
+                    : launch_rowdft<256>((const bf16*)in, rows, mat_packed, out, err, st, wait_cycles, 1);
 }
 
 int tt_fno_mix(int S, int B, int mode, const void* in, const void* w_packed, const void* a_packed, const float* sp,

@@ -2,19 +2,22 @@
 //
 // Replaces ElectronCube.solve / dsdt / dndr / ray_at_exit
 // (particle_tracking/particle_tracker.py:243-256, 312-380, 398-419).
-// One thread integrates one ray with its own RK45 instance that follows
-// scipy.integrate.solve_ivp(method='RK45') step for step: Dormand-Prince 5(4)
-// tableau, scipy's initial-step rule, RMS error norm over the ray's own
-// components, safety 0.9, step factors in [0.2, 10], exponent -1/5, step
-// clipped to t_bound, 10-ulp minimum step.  Lookups reproduce
-// RegularGridInterpolator(method='linear', fill_value=0) operation by
-// operation.  The file is compiled with -fmad=false so every product and sum
-// is rounded separately, as numpy does.
+// One thread integrates one ray with its own explicit Runge-Kutta instance
+// that follows scipy.integrate.solve_ivp step for step: RK45 (Dormand-Prince
+// 5(4), the reference's default method) built in, and any pair of the shapes
+// of scipy's RK23 (3 stages) and DOP853 (12 stages, E5/E3 error norm) from a
+// caller's tableau; scipy's initial-step rule, RMS error norm over the ray's
+// own components, safety 0.9, step factors in [0.2, 10], exponent
+// -1/(error order + 1), step clipped to t_bound, 10-spacing minimum step.
+// Lookups reproduce RegularGridInterpolator(method='linear', fill_value=0)
+// operation by operation.  The file is compiled with -fmad=false so every
+// product and sum is rounded separately, as numpy does.
 //
 // The reference integrates all rays as one system with one global step; a
 // per-ray step is the GPU-natural decomposition and converges to the same
 // trajectories (parity is asserted at tight tolerance).
 #include <math.h>
+#include <string.h>
 
 #include "tt_common.cuh"
 
@@ -58,17 +61,20 @@ __device__ inline int locate64(const double* __restrict__ g, int n, double g0, d
     return i;
 }
 
-// Trilinear lookup of nvol volumes at p.  Returns 0 = inside, 1 = outside
-// (values 0), 2 = NaN coordinate (values NaN).
-__device__ inline int lookup64(const Grid64& G, const Vols64& V, const double p[3], double out[4])
+// Trilinear lookup of the first NV volumes at p.  Returns 0 = inside,
+// 1 = outside (values 0), 2 = NaN coordinate (values NaN).
+template <int NV>
+__device__ inline int lookup64(const Grid64& G, const Vols64& V, const double p[3], double out[NV])
 {
     int idx[3];
     double d[3];
     int oob = 0;
+#pragma unroll
     for (int a = 0; a < 3; ++a) {
         const double v = p[a];
         if (v != v) {
-            for (int k = 0; k < V.nvol; ++k) out[k] = CUDART_NAN;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) out[k] = CUDART_NAN;
             return 2;
         }
         const double lo = __ldg(G.g[a]), hi = __ldg(G.g[a] + G.n[a] - 1);
@@ -78,11 +84,9 @@ __device__ inline int lookup64(const Grid64& G, const Vols64& V, const double p[
         const double gi = __ldg(G.g[a] + i);
         d[a] = (v - gi) / (__ldg(G.g[a] + i + 1) - gi);
     }
-    if (oob) {
-        for (int k = 0; k < V.nvol; ++k) out[k] = 0.0;
-        return 1;
-    }
-    for (int k = 0; k < V.nvol; ++k) out[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] = 0.0;
+    if (oob) return 1;
     const size_t base = (size_t)idx[0] * G.s0 + (size_t)idx[1] * G.s1 + (size_t)idx[2];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
@@ -92,7 +96,8 @@ __device__ inline int lookup64(const Grid64& G, const Vols64& V, const double p[
         w = w * (b ? d[1] : 1.0 - d[1]);
         w = w * (e ? d[2] : 1.0 - d[2]);
         const size_t off = base + (a ? G.s0 : 0) + (b ? G.s1 : 0) + (size_t)e;
-        for (int k = 0; k < V.nvol; ++k) out[k] = out[k] + __ldg(V.v[k] + off) * w;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) out[k] = out[k] + __ldg(V.v[k] + off) * w;
     }
     return 0;
 }
@@ -101,39 +106,39 @@ struct Cube64 {
     Grid64 G;
     Vols64 V;
     double k0;
-    int neq;
 };
 
-__device__ inline void rhs64(const Cube64& C, const double* y, double* f)
+// Right-hand side without the trivial rows: the accelerations (dv/dt = the
+// interpolated gradients, dsdt at particle_tracker.py:398-419) and, with
+// NEQ == 7, the phase rate k0 (n - 1) |v|.  Position rates are the velocity.
+template <int NEQ>
+__device__ inline void accel64(const Cube64& C, const double* pos, const double* vel, double* a)
 {
-    double g[4];
-    lookup64(C.G, C.V, y, g);
-    f[0] = y[3];
-    f[1] = y[4];
-    f[2] = y[5];
-    f[3] = g[0];
-    f[4] = g[1];
-    f[5] = g[2];
-    if (C.neq == 7) {
+    double g[NEQ == 7 ? 4 : 3];
+    lookup64<NEQ == 7 ? 4 : 3>(C.G, C.V, pos, g);
+    a[0] = g[0];
+    a[1] = g[1];
+    a[2] = g[2];
+    if (NEQ == 7) {
         const double q = g[3];
         double r = 1.0 - q;
         if (r < 0.0) r = 0.0;
         const double nm1 = -q / (1.0 + sqrt(r));
-        const double sp = sqrt(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
-        f[6] = C.k0 * nm1 * sp;
+        const double sp = sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+        a[3] = C.k0 * nm1 * sp;
     }
 }
 
-__constant__ double kA[6][5] = {
-    {0, 0, 0, 0, 0},
-    {1.0 / 5, 0, 0, 0, 0},
-    {3.0 / 40, 9.0 / 40, 0, 0, 0},
-    {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0},
-    {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0},
-    {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656}};
-__constant__ double kB[6] = {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84};
-__constant__ double kE[7] = {-71.0 / 57600, 0, 71.0 / 16695, -71.0 / 1920, 17253.0 / 339200,
-                             -22.0 / 525, 1.0 / 40};
+// An explicit Runge-Kutta pair as scipy's RungeKutta classes hold it (A, B,
+// C, E or DOP853's E5/E3) and its error order, in the kernel parameter bank.
+struct RKDev {
+    double a[TT_RK_MAX_STAGES][TT_RK_MAX_STAGES];
+    double b[TT_RK_MAX_STAGES];
+    double e[TT_RK_MAX_STAGES + 1];   // E, or E5 (DOP853)
+    double e3[TT_RK_MAX_STAGES + 1];  // DOP853 only
+    double err_exp;   // -1 / (error order + 1)
+    double init_exp;  //  1 / (error order + 1)
+};
 
 template <int NEQ>
 __device__ inline double rms(const double* v)
@@ -144,28 +149,38 @@ __device__ inline double rms(const double* v)
     return sqrt(s) / sqrt((double)NEQ);
 }
 
+// scipy.integrate._ivp.common.select_initial_step (Hairer, Norsett & Wanner,
+// Sec. II.4); f0 holds the accelerations (and phase rate) at y0.
 template <int NEQ>
-__device__ double initial_step64(const Cube64& C, const double* y0, const double* f0, double t_bound,
-                                 double rtol, double atol)
+__device__ double initial_step64(const Cube64& C, const RKDev& T, const double* y0, const double* f0,
+                                 double t_bound, double rtol, double atol)
 {
-    double sc[NEQ], tmp[NEQ], y1[NEQ], f1[NEQ];
+    constexpr int NA = NEQ - 3;
+    double sc[NEQ], tmp[NEQ], f[NEQ];
     const double L = fabs(t_bound);
     if (L == 0.0) return 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) f[i] = y0[3 + i];
+#pragma unroll
+    for (int i = 0; i < NA; ++i) f[3 + i] = f0[i];
 #pragma unroll
     for (int i = 0; i < NEQ; ++i) sc[i] = atol + fabs(y0[i]) * rtol;
 #pragma unroll
     for (int i = 0; i < NEQ; ++i) tmp[i] = y0[i] / sc[i];
     const double d0 = rms<NEQ>(tmp);
 #pragma unroll
-    for (int i = 0; i < NEQ; ++i) tmp[i] = f0[i] / sc[i];
+    for (int i = 0; i < NEQ; ++i) tmp[i] = f[i] / sc[i];
     const double d1 = rms<NEQ>(tmp);
     double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
     if (h0 > L) h0 = L;
+    double y1[NEQ], f1[NA];
 #pragma unroll
-    for (int i = 0; i < NEQ; ++i) y1[i] = y0[i] + h0 * f0[i];
-    rhs64(C, y1, f1);
+    for (int i = 0; i < NEQ; ++i) y1[i] = y0[i] + h0 * f[i];
+    accel64<NEQ>(C, y1, y1 + 3, f1);
 #pragma unroll
-    for (int i = 0; i < NEQ; ++i) tmp[i] = (f1[i] - f0[i]) / sc[i];
+    for (int i = 0; i < 3; ++i) tmp[i] = (y1[3 + i] - f[i]) / sc[i];
+#pragma unroll
+    for (int i = 0; i < NA; ++i) tmp[3 + i] = (f1[i] - f[3 + i]) / sc[3 + i];
     const double d2 = rms<NEQ>(tmp) / h0;
     double h1;
     if (d1 <= 1e-15 && d2 <= 1e-15) {
@@ -173,7 +188,7 @@ __device__ double initial_step64(const Cube64& C, const double* y0, const double
         if (h1 < 1e-6) h1 = 1e-6;
     } else {
         const double m = d1 > d2 ? d1 : d2;
-        h1 = pow(0.01 / m, 1.0 / 5.0);
+        h1 = pow(0.01 / m, T.init_exp);
     }
     double h = 100.0 * h0;
     if (h1 < h) h = h1;
@@ -181,16 +196,22 @@ __device__ double initial_step64(const Cube64& C, const double* y0, const double
     return h;
 }
 
-template <int NEQ>
-__device__ int integrate64(const Cube64& C, double* y, double t_bound, double rtol, double atol,
+// One ray through scipy's RungeKutta._step_impl loop (safety 0.9, factors in
+// [0.2, 10], RMS norm, step clipped to t_bound, TOO_SMALL below 10 spacings of
+// t).  NS stages per step plus the FSAL evaluation at the new point; DOP853
+// (DOP = true) takes scipy's combined E5/E3 error norm.
+template <int NS, bool DOP, int NEQ>
+__device__ int integrate64(const Cube64& C, const RKDev& T, double* y, double t_bound, double rtol, double atol,
                            long long max_steps, int* nacc_out)
 {
-    double f[NEQ], K[7][NEQ], yn[NEQ], ys[NEQ];
+    double K[NS + 1][NEQ];
     for (int i = 0; i < NEQ; ++i)
         if (!isfinite(y[i])) { *nacc_out = 0; return TT_RAY_NAN; }
-    rhs64(C, y, f);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) K[0][i] = y[3 + i];
+    accel64<NEQ>(C, y, y + 3, &K[0][3]);
     long long nacc = 0, natt = 0;
-    double h_abs = initial_step64<NEQ>(C, y, f, t_bound, rtol, atol);
+    double h_abs = initial_step64<NEQ>(C, T, y, &K[0][3], t_bound, rtol, atol);
     double t = 0.0;
     int code = TT_RAY_OK;
     if (t != t_bound) {
@@ -199,6 +220,7 @@ __device__ int integrate64(const Cube64& C, double* y, double t_bound, double rt
             if (h_abs < min_step) h_abs = min_step;
             bool rejected = false;
             double t_new;
+            double yn[NEQ];
             for (;;) {
                 if (h_abs < min_step) { code = TT_RAY_STEP_TOO_SMALL; break; }
                 if (natt >= max_steps) { code = TT_RAY_MAX_STEPS; break; }
@@ -209,50 +231,68 @@ __device__ int integrate64(const Cube64& C, double* y, double t_bound, double rt
                 h = t_new - t;
                 h_abs = fabs(h);
 #pragma unroll
-                for (int i = 0; i < NEQ; ++i) K[0][i] = f[i];
+                for (int s = 1; s < NS; ++s) {
+                    double ys[6];
 #pragma unroll
-                for (int s = 1; s < 6; ++s) {
-#pragma unroll
-                    for (int i = 0; i < NEQ; ++i) {
+                    for (int i = 0; i < 6; ++i) {
                         double acc = 0.0;
 #pragma unroll
-                        for (int j = 0; j < s; ++j) acc += K[j][i] * kA[s][j];
+                        for (int j = 0; j < s; ++j) acc += K[j][i] * T.a[s][j];
                         ys[i] = y[i] + acc * h;
                     }
-                    rhs64(C, ys, K[s]);
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) K[s][i] = ys[3 + i];
+                    accel64<NEQ>(C, ys, ys + 3, &K[s][3]);
                 }
 #pragma unroll
                 for (int i = 0; i < NEQ; ++i) {
                     double acc = 0.0;
 #pragma unroll
-                    for (int j = 0; j < 6; ++j) acc += K[j][i] * kB[j];
+                    for (int j = 0; j < NS; ++j) acc += K[j][i] * T.b[j];
                     yn[i] = y[i] + h * acc;
                 }
-                rhs64(C, yn, K[6]);
-                double es = 0.0;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) K[NS][i] = yn[3 + i];
+                accel64<NEQ>(C, yn, yn + 3, &K[NS][3]);
+                double e5s = 0.0, e3s = 0.0;
 #pragma unroll
                 for (int i = 0; i < NEQ; ++i) {
                     const double ay = fabs(y[i]), an = fabs(yn[i]);
                     const double sc = atol + (ay > an ? ay : an) * rtol;
-                    double acc = 0.0;
+                    double acc = 0.0, acc3 = 0.0;
 #pragma unroll
-                    for (int j = 0; j < 7; ++j) acc += K[j][i] * kE[j];
-                    const double e = acc * h / sc;
-                    es += e * e;
+                    for (int j = 0; j <= NS; ++j) {
+                        acc += K[j][i] * T.e[j];
+                        if (DOP) acc3 += K[j][i] * T.e3[j];
+                    }
+                    if (DOP) {
+                        const double x5 = acc / sc, x3 = acc3 / sc;
+                        e5s += x5 * x5;
+                        e3s += x3 * x3;
+                    } else {
+                        const double e = acc * h / sc;
+                        e5s += e * e;
+                    }
                 }
-                const double en = sqrt(es) / sqrt((double)NEQ);
+                double en;
+                if (DOP) {
+                    if (e5s == 0.0 && e3s == 0.0) en = 0.0;
+                    else en = fabs(h) * e5s / sqrt((e5s + 0.01 * e3s) * (double)NEQ);
+                } else {
+                    en = sqrt(e5s) / sqrt((double)NEQ);
+                }
                 if (en < 1.0) {
                     double factor;
                     if (en == 0.0) factor = 10.0;
                     else {
-                        factor = 0.9 * pow(en, -0.2);
+                        factor = 0.9 * pow(en, T.err_exp);
                         if (!(factor < 10.0)) factor = 10.0;
                     }
                     if (rejected && !(factor < 1.0)) factor = 1.0;
                     h_abs *= factor;
                     break;
                 } else {
-                    double factor = 0.9 * pow(en, -0.2);
+                    double factor = 0.9 * pow(en, T.err_exp);
                     if (!(factor > 0.2)) factor = 0.2;
                     h_abs *= factor;
                     rejected = true;
@@ -262,7 +302,10 @@ __device__ int integrate64(const Cube64& C, double* y, double t_bound, double rt
             ++nacc;
             t = t_new;
 #pragma unroll
-            for (int i = 0; i < NEQ; ++i) { y[i] = yn[i]; f[i] = K[6][i]; }
+            for (int i = 0; i < NEQ; ++i) {
+                y[i] = yn[i];
+                K[0][i] = K[NS][i];
+            }
             if (t - t_bound >= 0) break;
         }
     }
@@ -295,13 +338,20 @@ __device__ inline void ray_at_exit64(const double* y, int axis, double extent, d
     }
 }
 
-template <int NEQ>
-__global__ void __launch_bounds__(128, 1) trace64_kernel(Cube64 C, const double* __restrict__ s0, long long np,
-                                                      double t_end, int axis, double extent, double rtol,
-                                                      double atol, long long max_steps,
-                                                      double* __restrict__ sf, double* __restrict__ rf,
-                                                      double* __restrict__ phase, int* __restrict__ status,
-                                                      int* __restrict__ nsteps)
+// Resident blocks of 128 per SM the register budget of each instantiation is
+// sized for: 3 for RK23 / RK45 (168 registers with phase, no spill), 2 for
+// DOP853's 13 stored stages.
+template <int NS, int NEQ>
+struct Occ64 {
+    static constexpr int blocks = NS <= 6 ? 3 : 2;
+};
+
+template <int NS, bool DOP, int NEQ>
+__global__ void __launch_bounds__(128, Occ64<NS, NEQ>::blocks)
+trace64_kernel(Cube64 C, const __grid_constant__ RKDev T, const double* __restrict__ s0, long long np,
+               double t_end, int axis, double extent, double rtol, double atol, long long max_steps,
+               double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
+               int* __restrict__ status, int* __restrict__ nsteps)
 {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < np;
          r += (long long)gridDim.x * blockDim.x) {
@@ -310,7 +360,7 @@ __global__ void __launch_bounds__(128, 1) trace64_kernel(Cube64 C, const double*
         for (int i = 0; i < 6; ++i) y[i] = s0[(size_t)i * np + r];
         if (NEQ == 7) y[NEQ - 1] = 0.0;
         int nacc = 0;
-        const int code = integrate64<NEQ>(C, y, t_end, rtol, atol, max_steps, &nacc);
+        const int code = integrate64<NS, DOP, NEQ>(C, T, y, t_end, rtol, atol, max_steps, &nacc);
         if (sf) {
 #pragma unroll
             for (int i = 0; i < 6; ++i) sf[(size_t)i * np + r] = y[i];
@@ -327,15 +377,17 @@ __global__ void __launch_bounds__(128, 1) trace64_kernel(Cube64 C, const double*
     }
 }
 
+template <int NV>
 __global__ void dndr_kernel(Grid64 G, Vols64 V, const double* __restrict__ pts, long long npts,
                             double* __restrict__ out)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npts;
          i += (long long)gridDim.x * blockDim.x) {
         double p[3] = {pts[i], pts[npts + i], pts[2 * npts + i]};
-        double o[4];
-        lookup64(G, V, p, o);
-        for (int k = 0; k < V.nvol; ++k) out[(size_t)k * npts + i] = o[k];
+        double o[NV];
+        lookup64<NV>(G, V, p, o);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) out[(size_t)k * npts + i] = o[k];
     }
 }
 
@@ -379,15 +431,104 @@ extern "C" int tt_dndr(const double* const* vols, int nvol, int nx, int ny, int 
     for (int k = 0; k < 4; ++k) V.v[k] = k < nvol ? vols[k] : nullptr;
     for (int k = 0; k < nvol; ++k)
         if (!V.v[k]) return tt::invalid("dndr: null volume");
-    dndr_kernel<<<grid_size(npts, 256), 256, 0, tt::as_stream(stream)>>>(G, V, pts, npts, out);
+    const int g = grid_size(npts, 256);
+    cudaStream_t st = tt::as_stream(stream);
+    switch (nvol) {
+        case 1: dndr_kernel<1><<<g, 256, 0, st>>>(G, V, pts, npts, out); break;
+        case 2: dndr_kernel<2><<<g, 256, 0, st>>>(G, V, pts, npts, out); break;
+        case 3: dndr_kernel<3><<<g, 256, 0, st>>>(G, V, pts, npts, out); break;
+        default: dndr_kernel<4><<<g, 256, 0, st>>>(G, V, pts, npts, out); break;
+    }
     return tt::launch_status("dndr kernel");
 }
 
-extern "C" int tt_trace_f64(const double* dndx, const double* dndy, const double* dndz, const double* ne_nc,
-                            int nx, int ny, int nz, const double* x, const double* y, const double* z,
-                            double omega, const double* s0, int64_t np, double t_end, int probing_axis,
-                            double extent, const tt_trace_opts* opts, double* sf, double* rf,
-                            double* phase, int32_t* status, int32_t* nsteps, void* stream)
+namespace {
+
+// Dormand-Prince 5(4) as scipy's RK45 holds it (Dormand & Prince 1980).
+tt_rk_tableau dp54()
+{
+    tt_rk_tableau t{};
+    t.n_stages = 6;
+    t.error_order = 4;
+    t.error_kind = 0;
+    const double C[6] = {0.0, 1.0 / 5, 3.0 / 10, 4.0 / 5, 8.0 / 9, 1.0};
+    const double A[6][5] = {
+        {0, 0, 0, 0, 0},
+        {1.0 / 5, 0, 0, 0, 0},
+        {3.0 / 40, 9.0 / 40, 0, 0, 0},
+        {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0},
+        {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0},
+        {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656}};
+    const double B[6] = {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84};
+    const double E[7] = {-71.0 / 57600, 0, 71.0 / 16695, -71.0 / 1920, 17253.0 / 339200, -22.0 / 525, 1.0 / 40};
+    for (int s = 0; s < 6; ++s) {
+        t.C[s] = C[s];
+        t.B[s] = B[s];
+        for (int k = 0; k < 5; ++k) t.A[s][k] = A[s][k];
+    }
+    for (int s = 0; s < 7; ++s) t.E[s] = E[s];
+    return t;
+}
+
+// Checks a caller's tableau and forms the device copy.
+int make_rkdev(const tt_rk_tableau* t, RKDev* D)
+{
+    const int ns = t->n_stages;
+    if (!(ns == 3 || ns == 6 || ns == 12))
+        return tt::invalid("trace_f64: n_stages must be 3, 6 or 12 (RK23, RK45, DOP853 forms)");
+    if (t->error_kind != 0 && t->error_kind != 1) return tt::invalid("trace_f64: error_kind must be 0 or 1");
+    if ((t->error_kind == 1) != (ns == 12))
+        return tt::invalid("trace_f64: the E5/E3 error norm (error_kind 1) goes with 12 stages");
+    if (t->error_order < 1 || t->error_order > 16) return tt::invalid("trace_f64: error_order must be 1..16");
+    for (int s = 0; s < ns; ++s) {
+        double rs = 0.0;
+        for (int k = 0; k < s; ++k) rs += t->A[s][k];
+        for (int k = s; k < TT_RK_MAX_STAGES; ++k)
+            if (t->A[s][k] != 0.0) return tt::invalid("trace_f64: A must be strictly lower triangular");
+        if (fabs(rs - t->C[s]) > 1e-12) return tt::invalid("trace_f64: row sums of A must equal C");
+    }
+    double sb = 0.0, se = 0.0, se3 = 0.0;
+    for (int s = 0; s < ns; ++s) sb += t->B[s];
+    for (int s = 0; s <= ns; ++s) {
+        se += t->E[s];
+        se3 += t->E3[s];
+    }
+    if (fabs(sb - 1.0) > 1e-12 || fabs(se) > 1e-12 || (t->error_kind == 1 && fabs(se3) > 1e-12))
+        return tt::invalid("trace_f64: B must sum to 1 and E to 0");
+    RKDev d;
+    memset(&d, 0, sizeof(d));
+    for (int s = 0; s < ns; ++s) {
+        d.b[s] = t->B[s];
+        for (int k = 0; k < ns; ++k) d.a[s][k] = t->A[s][k];
+    }
+    for (int k = 0; k <= ns; ++k) {
+        d.e[k] = t->E[k];
+        d.e3[k] = t->error_kind == 1 ? t->E3[k] : 0.0;
+    }
+    d.err_exp = -1.0 / (t->error_order + 1);
+    d.init_exp = 1.0 / (t->error_order + 1);
+    *D = d;
+    return TT_OK;
+}
+
+template <int NS, bool DOP>
+void launch64(bool phase, const Cube64& C, const RKDev& T, const double* s0, long long np, double t_end, int axis,
+              double extent, const tt_trace_opts* o, long long maxs, double* sf, double* rf, double* ph, int* st,
+              int* ns, cudaStream_t s)
+{
+    const int block = 128;
+    if (phase)
+        trace64_kernel<NS, DOP, 7><<<grid_size(np, block), block, 0, s>>>(C, T, s0, np, t_end, axis, extent, o->rtol,
+                                                                         o->atol, maxs, sf, rf, ph, st, ns);
+    else
+        trace64_kernel<NS, DOP, 6><<<grid_size(np, block), block, 0, s>>>(C, T, s0, np, t_end, axis, extent, o->rtol,
+                                                                         o->atol, maxs, sf, rf, ph, st, ns);
+}
+
+int trace64(const double* dndx, const double* dndy, const double* dndz, const double* ne_nc, int nx, int ny, int nz,
+            const double* x, const double* y, const double* z, double omega, const double* s0, int64_t np,
+            double t_end, int probing_axis, double extent, const tt_trace_opts* opts, const tt_rk_tableau* tab,
+            double* sf, double* rf, double* phase, int32_t* status, int32_t* nsteps, void* stream)
 {
     if (!opts) return tt::invalid("trace_f64: opts is null");
     if (!dndx || !dndy || !dndz || !x || !y || !z) return tt::invalid("trace_f64: null pointer");
@@ -397,6 +538,8 @@ extern "C" int tt_trace_f64(const double* dndx, const double* dndy, const double
     if (np < 0) return tt::invalid("trace_f64: np < 0");
     if (!(opts->rtol > 0.0) || !(opts->atol >= 0.0)) return tt::invalid("trace_f64: need rtol > 0, atol >= 0");
     if (!(t_end >= 0.0)) return tt::invalid("trace_f64: t_end must be >= 0");
+    RKDev T;
+    TT_TRY(make_rkdev(tab, &T));
     if (np == 0) return TT_OK;
     if (!s0) return tt::invalid("trace_f64: s0 is null");
     Cube64 C;
@@ -407,17 +550,39 @@ extern "C" int tt_trace_f64(const double* dndx, const double* dndy, const double
     C.V.v[3] = ne_nc;
     C.V.nvol = opts->with_phase ? 4 : 3;
     C.k0 = omega / TT_C_LIGHT;
-    C.neq = opts->with_phase ? 7 : 6;
     const long long maxs = opts->max_steps > 0 ? opts->max_steps : TT_DEFAULT_MAX_STEPS;
     cudaStream_t s = tt::as_stream(stream);
-    const int block = 128;
-    if (opts->with_phase)
-        trace64_kernel<7><<<grid_size(np, block), block, 0, s>>>(C, s0, np, t_end, probing_axis, extent,
-                                                                 opts->rtol, opts->atol, maxs, sf, rf, phase,
-                                                                 status, nsteps);
+    const bool ph = opts->with_phase != 0;
+    if (tab->n_stages == 3)
+        launch64<3, false>(ph, C, T, s0, np, t_end, probing_axis, extent, opts, maxs, sf, rf, phase, status, nsteps, s);
+    else if (tab->n_stages == 6)
+        launch64<6, false>(ph, C, T, s0, np, t_end, probing_axis, extent, opts, maxs, sf, rf, phase, status, nsteps, s);
     else
-        trace64_kernel<6><<<grid_size(np, block), block, 0, s>>>(C, s0, np, t_end, probing_axis, extent,
-                                                                 opts->rtol, opts->atol, maxs, sf, rf, phase,
-                                                                 status, nsteps);
+        launch64<12, true>(ph, C, T, s0, np, t_end, probing_axis, extent, opts, maxs, sf, rf, phase, status, nsteps,
+                           s);
     return tt::launch_status("trace_f64 kernel");
+}
+
+}  // namespace
+
+extern "C" int tt_trace_f64(const double* dndx, const double* dndy, const double* dndz, const double* ne_nc,
+                            int nx, int ny, int nz, const double* x, const double* y, const double* z,
+                            double omega, const double* s0, int64_t np, double t_end, int probing_axis,
+                            double extent, const tt_trace_opts* opts, double* sf, double* rf,
+                            double* phase, int32_t* status, int32_t* nsteps, void* stream)
+{
+    static const tt_rk_tableau T = dp54();
+    return trace64(dndx, dndy, dndz, ne_nc, nx, ny, nz, x, y, z, omega, s0, np, t_end, probing_axis, extent, opts,
+                   &T, sf, rf, phase, status, nsteps, stream);
+}
+
+extern "C" int tt_trace_f64_rk(const double* dndx, const double* dndy, const double* dndz, const double* ne_nc,
+                               int nx, int ny, int nz, const double* x, const double* y, const double* z,
+                               double omega, const double* s0, int64_t np, double t_end, int probing_axis,
+                               double extent, const tt_trace_opts* opts, const tt_rk_tableau* tableau, double* sf,
+                               double* rf, double* phase, int32_t* status, int32_t* nsteps, void* stream)
+{
+    if (!tableau) return tt::invalid("trace_f64_rk: tableau is null");
+    return trace64(dndx, dndy, dndz, ne_nc, nx, ny, nz, x, y, z, omega, s0, np, t_end, probing_axis, extent, opts,
+                   tableau, sf, rf, phase, status, nsteps, stream);
 }

@@ -9,12 +9,17 @@ rad on the exit plane.
 
 Additions (keyword-only, defaults keep the reference behaviour):
   solve(method='RK45', rtol=None, atol=None, precision='fp64', phase=False, max_steps=None)
-    precision='fp64'  plain drop-in: per-ray RK45 with scipy's controller,
-                      rtol/atol default to solve_ivp's 1e-3 / 1e-6;
+    precision='fp64'  plain drop-in: per-ray RK45 (or solve_ivp's RK23 / DOP853)
+                      with scipy's controller, rtol/atol default to solve_ivp's
+                      1e-3 / 1e-6;
     precision='fp32'  persistent FP32 tracer (uniform grids), rtol default 1e-7
                       on velocity/phase, atol default 1e-5 cells;
     phase=True        also integrates k0 * int (n - 1) ds into self.phase.
-  set_up_interps()    (re)builds the device lookup state; calc_dndr calls it.
+  set_up_interps()    (re)builds the FP64 device lookup state now (calc_dndr
+                      defers it to first use).
+  rf, phase, status and nsteps from a solve of host rays are read-only numpy
+  arrays that keep their device copies (setflags(write=True) before writing
+  into one in place).
   self.status, self.nsteps  per-ray outcome and accepted-step count.
 """
 from datetime import datetime
@@ -93,13 +98,20 @@ class ElectronCube:
 
     # --- gradient and lookups (particle_tracker.py:220-256)
     def calc_dndr(self, lwl=1053e-9, ne_max=1):
-        """Gradient of n_e/n_c times -c^2/2 on the GPU; builds the lookups."""
+        """Gradient of n_e/n_c times -c^2/2 on the GPU; builds the lookups.
+        The FP64 arrays are formed when first used (the FP64 solve, dndr, the
+        ne_nc/dndx/dndy/dndz attributes); the FP32 tracer builds its own
+        volume from ne, so a precision='fp32' solve never forms them."""
         self._dndr_args = (lwl, ne_max)
-        self.set_up_interps()
+        self._dev = None
+        self._vol32 = None
+        self._host_cache = {}
+        self.omega = 2 * np.pi * (c / lwl)  # particle_tracker.py:227
+        self._interps()
 
     def set_up_interps(self):
-        """(Re)build the device state: FP64 ne_nc and gradients (bit-identical to
-        numpy), and the trilinear lookups.  Idempotent."""
+        """(Re)build the device state now: FP64 ne_nc and gradients
+        (bit-identical to numpy) and the trilinear lookups.  Idempotent."""
         if self._dndr_args is None:
             raise RuntimeError("call calc_dndr(lwl, ne_max) first")
         lwl, ne_max = self._dndr_args
@@ -108,6 +120,9 @@ class ElectronCube:
         self._vol32 = None
         self._host_cache = {}
         self.omega = f["omega"]
+        self._interps()
+
+    def _interps(self):
         self.dndx_interp = _DeviceInterp(self, "dndx")
         self.dndy_interp = _DeviceInterp(self, "dndy")
         self.dndz_interp = _DeviceInterp(self, "dndz")
@@ -200,8 +215,16 @@ class ElectronCube:
 
     # --- integration (particle_tracker.py:312-331)
     def solve(self, method="RK45", *, rtol=None, atol=None, precision="fp64", phase=False, max_steps=None):
-        if method != "RK45":
-            raise NotImplementedError("only method='RK45' (Dormand-Prince 5(4)) is implemented on the GPU")
+        """Trace self.s0 to t_end (particle_tracker.py:312-331).  method is
+        solve_ivp's: 'RK45' (default), 'RK23', 'DOP853' or an explicit
+        RungeKutta subclass, integrated per ray in FP64 with scipy's step
+        control; the implicit methods (Radau, BDF, LSODA) raise
+        NotImplementedError.  precision='fp32' is the persistent FP32 tracer,
+        which integrates RK45 only."""
+        if precision == "fp32" and not (isinstance(method, str) and method == "RK45"):
+            raise NotImplementedError("precision='fp32' integrates RK45 (Dormand-Prince 5(4)) only")
+        if precision == "fp64" and not (isinstance(method, str) and method == "RK45"):
+            core.rk_tableau(method)  # raises for methods the GPU does not integrate
         extent = self._extent()
         t = np.linspace(0.0, np.sqrt(8.0) * extent / c, 2)
         t_end = t[-1]
@@ -210,9 +233,10 @@ class ElectronCube:
         if precision == "fp64":
             out = core.trace_f64(self._fields(), self.s0, t_end, _AXIS[self.probing_direction], extent,
                                  rtol=1e-3 if rtol is None else rtol, atol=1e-6 if atol is None else atol,
-                                 phase=phase, max_steps=max_steps)
+                                 phase=phase, max_steps=max_steps, method=method)
         elif precision == "fp32":
-            self._fields()
+            if self._dndr_args is None:
+                raise RuntimeError("call calc_dndr(lwl, ne_max) first")
             out = core.trace_f32(self.volume32(), self.s0, t_end, extent,
                                  rtol=1e-7 if rtol is None else rtol, atol=1e-5 if atol is None else atol,
                                  phase=phase, max_steps=max_steps)
@@ -221,7 +245,9 @@ class ElectronCube:
         torch.cuda.current_stream().synchronize()
         finish = time()
         print("Ray trace completed in:\t", finish - start, "s")
-        conv = (lambda t_: t_) if on_device else core.to_host
+        # host rays in -> host arrays out; rf and phase keep their device copies
+        # as twins (read-only arrays), so diagnostics given them upload nothing
+        conv = (lambda t_: t_) if on_device else (lambda t_: core.to_host(t_, twin=True))
         if on_device:
             self.sf = out["sf"]
         else:

@@ -32,6 +32,7 @@ def _run_chain(r, ops, inplace):
         return out
     host = out.cpu().numpy()
     if inplace:
+        core.release_twin(r)  # an in-place filter on a solve() result: writeable again, twin dropped
         r[...] = host
         return r
     return host

@@ -148,6 +148,9 @@ typedef struct tt_trace_opts {
     int32_t block_size; /* FP32 tracer: threads per block, 64, 128 or 256 (0 = 256) */
     int32_t ray_chunk;  /* FP32 tracer: consecutive (bucketed) rays a warp takes from the work
                            counter at a time, a multiple of 32 up to 1024; 0 = 32 */
+    int32_t phase_f64;  /* FP32 tracer with phase: accumulate the phase sum in FP64 (one double add
+                           per accepted step) instead of a Neumaier-compensated FP32 pair */
+    int32_t reserved;
 } tt_trace_opts;
 
 /* Plain FP64 drop-in: scipy RK45 controller per ray (safety 0.9, factors

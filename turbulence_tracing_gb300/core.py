@@ -213,8 +213,9 @@ def rebuild_volume(vol):
 # ---------------------------------------------------------------------------
 # K2
 # ---------------------------------------------------------------------------
-def _opts(rtol, atol, atol_phase, max_steps, with_phase, block_size=0, ray_chunk=0):
+def _opts(rtol, atol, atol_phase, max_steps, with_phase, block_size=0, ray_chunk=0, phase_f64=False):
     o = _lib.TTTraceOpts()
+    o.phase_f64 = 1 if phase_f64 else 0
     o.rtol = float(rtol)
     o.atol = float(atol)
     o.atol_phase = float(atol_phase)
@@ -303,8 +304,9 @@ def trace_f64(fields, s0, t_end, probing_axis, extent, rtol=1e-3, atol=1e-6, pha
 
 
 def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, phase=False, max_steps=None,
-              want_sf=True, ws=None, out=None, block_size=0, ray_chunk=0):
-    """Persistent FP32 tracer over a Volume32.  s0: (6, Np) float64."""
+              want_sf=True, ws=None, out=None, block_size=0, ray_chunk=0, phase_f64=False):
+    """Persistent FP32 tracer over a Volume32.  s0: (6, Np) float64.
+    phase_f64: accumulate the phase in FP64 rather than a compensated FP32 pair."""
     dev = require_cuda()
     L = _lib.lib()
     s0_t = _f64_dev(s0, dev)
@@ -316,7 +318,7 @@ def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, pha
     need = L.tt_trace_f32_workspace_bytes(ctypes.byref(vol.desc), np_)
     if ws is None or ws.numel() < need:
         ws = workspace(need, dev)
-    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size, ray_chunk)
+    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size, ray_chunk, phase_f64)
     check(L.tt_trace_f32(ctypes.byref(vol.desc), _ptr(s0_t), np_, float(t_end), float(extent), ctypes.byref(o),
                          _ptr(out["sf"]), _ptr(out["rf"]), _ptr(out["phase"]) if phase else None,
                          _ptr(out["status"]), _ptr(out["nsteps"]), _ptr(ws), ws.numel(), _stream()),

@@ -16,7 +16,8 @@
 // a face is redone ending at the crossing.  Outside the box the ray is a
 // straight line, finished analytically.  Error control per ray (scipy's
 // controller constants) on position (cells), direction and phase.  Path
-// length and phase are compensated sums.  The interpolant and the stage
+// length and phase are compensated sums (the phase optionally an FP64 sum:
+// one double add per accepted step, the stage arithmetic staying FP32).  The interpolant and the stage
 // combinations of the two transverse components run as packed FP32x2 FMAs
 // (__ffma2_rn: per lane the same rounding as fmaf, so results are unchanged).
 //
@@ -135,6 +136,7 @@ struct Geo {
 struct Ctl {
     float rtol, inv_rtol, inv_atol_cells, atol_phase;
     int with_phase;
+    int phase_f64;  // accumulate the phase in FP64 (else a Neumaier-compensated FP32 pair)
     int chunk;  // rays a warp takes from the work counter at a time (>= 32)
     long long max_steps;
 };
@@ -161,18 +163,8 @@ __device__ __forceinline__ int tile_key(const Geo& G, int ta, int tb)
     return (sa * G.st_b + sb) * 64 + (int)m;
 }
 
-__device__ __forceinline__ float tri(const float* c, float fa, float fb, float fc)
-{
-    const float t1 = fmaf(c[7], fc, c[4]);
-    const float t2 = fmaf(c[5], fc, c[1]);
-    const float t3 = fmaf(fb, t1, t2);
-    const float t4 = fmaf(c[6], fc, c[2]);
-    const float t5 = fmaf(c[3], fc, c[0]);
-    const float t6 = fmaf(fb, t4, t5);
-    return fmaf(fa, t3, t6);
-}
-
-// tri() on two components at once (packed FP32x2; each lane's arithmetic is tri's).
+// The trilinear polynomial of two components at once (packed FP32x2):
+//   c0 + fc c3 + fb (c2 + fc c6) + fa ((c1 + fc c5) + fb (c4 + fc c7)).
 __device__ __forceinline__ float2 tri2(const float2* c, float fa, float fb, float fc)
 {
     const float2 A = make_float2(fa, fa), Bv = make_float2(fb, fb), Cv = make_float2(fc, fc);
@@ -185,19 +177,33 @@ __device__ __forceinline__ float2 tri2(const float2* c, float fa, float fb, floa
     return __ffma2_rn(A, t3, t6);
 }
 
-// Polynomial coefficients of the trilinear interpolant of one component.
-__device__ __forceinline__ void poly(float v000, float v001, float v010, float v011, float v100, float v101,
-                                     float v110, float v111, float* c)
+// a - b lane-wise, rounded as the scalar subtraction (fma(b, -1, a) is exact up to its one rounding)
+__device__ __forceinline__ float2 sub2(float2 a, float2 b)
+{
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+
+// Polynomial coefficients of the trilinear interpolant of two components at
+// once (packed FP32x2; lane-wise the scalar differences
+//   c0 = v000, c1 = v100 - v000, c2 = v010 - v000, c3 = v001 - v000,
+//   c4 = (v110 - v100) - c2, c5 = (v101 - v100) - c3, c6 = (v011 - v010) - c3,
+//   c7 = ((v111 - v110) - (v101 - v100)) - c6).
+__device__ __forceinline__ void poly2(float2 v000, float2 v001, float2 v010, float2 v011, float2 v100, float2 v101,
+                                      float2 v110, float2 v111, float2* c)
 {
     c[0] = v000;
-    c[1] = v100 - v000;
-    c[2] = v010 - v000;
-    c[3] = v001 - v000;
-    c[4] = (v110 - v100) - (v010 - v000);
-    c[5] = (v101 - v100) - (v001 - v000);
-    c[6] = (v011 - v010) - (v001 - v000);
-    c[7] = ((v111 - v110) - (v101 - v100)) - ((v011 - v010) - (v001 - v000));
+    c[1] = sub2(v100, v000);
+    c[2] = sub2(v010, v000);
+    c[3] = sub2(v001, v000);
+    const float2 d101 = sub2(v101, v100);
+    c[4] = sub2(sub2(v110, v100), c[2]);
+    c[5] = sub2(d101, c[3]);
+    c[6] = sub2(sub2(v011, v010), c[3]);
+    c[7] = sub2(sub2(sub2(v111, v110), d101), c[6]);
 }
+
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 
 __device__ __forceinline__ void load_cell(const Geo& G, const float4* __restrict__ nodes, long long tbase, int ca,
                                           int cb, int cc, float2 (*coef)[8])
@@ -211,16 +217,8 @@ __device__ __forceinline__ void load_cell(const Geo& G, const float4* __restrict
     const float4 n010 = __ldg(p + db), n011 = __ldg(p + db + dc);
     const float4 n100 = __ldg(p + da), n101 = __ldg(p + da + dc);
     const float4 n110 = __ldg(p + da + db), n111 = __ldg(p + da + db + dc);
-    float cx[8], cy[8], cz[8], cw[8];
-    poly(n000.x, n001.x, n010.x, n011.x, n100.x, n101.x, n110.x, n111.x, cx);
-    poly(n000.y, n001.y, n010.y, n011.y, n100.y, n101.y, n110.y, n111.y, cy);
-    poly(n000.z, n001.z, n010.z, n011.z, n100.z, n101.z, n110.z, n111.z, cz);
-    poly(n000.w, n001.w, n010.w, n011.w, n100.w, n101.w, n110.w, n111.w, cw);
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        coef[0][i] = make_float2(cx[i], cy[i]);
-        coef[1][i] = make_float2(cz[i], cw[i]);
-    }
+    poly2(lo2(n000), lo2(n001), lo2(n010), lo2(n011), lo2(n100), lo2(n101), lo2(n110), lo2(n111), coef[0]);
+    poly2(hi2(n000), hi2(n001), hi2(n010), hi2(n011), hi2(n100), hi2(n101), hi2(n110), hi2(n111), coef[1]);
 }
 
 __device__ __forceinline__ float nm1f(float q)
@@ -244,7 +242,7 @@ struct Ray {
     float fr[3];
     float u[3];
     float sig, sigc;
-    float ph, phc;
+    float ph, phc;   // phase: Neumaier pair, or (FP64 accumulation) the two words of one double
     float hctrl;
     float hcap;    // one-shot cap on the next attempt after a face-crossing rejection
     int natt, nacc;
@@ -256,6 +254,18 @@ struct Ray {
     int ta, tb;
     long long tbase;
 };
+
+// The FP64 phase accumulator kept in the registers of the (ph, phc) pair.
+__device__ __forceinline__ double ph_get(const Ray& R)
+{
+    return __hiloint2double(__float_as_int(R.ph), __float_as_int(R.phc));
+}
+
+__device__ __forceinline__ void ph_set(Ray& R, double v)
+{
+    R.ph = __int_as_float(__double2hiint(v));
+    R.phc = __int_as_float(__double2loint(v));
+}
 
 // Interior faces: a stage may use the current cell's polynomial up to kTolE
 // cells past a face, and a step may run at most kFacePath (path, in cells) past
@@ -458,7 +468,7 @@ template <bool ENTERED>
 __device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const Ray& R, const double* P0,
                                            const double* u0, long long r, long long np, double* __restrict__ sf,
                                            double* __restrict__ rf, double* __restrict__ phase,
-                                           int* __restrict__ status, int* __restrict__ nsteps)
+                                           int* __restrict__ status, int* __restrict__ nsteps, bool ph64)
 {
     // Position/velocity where stepping stopped, then the straight-line flight to
     // t_end for rays outside the box (zero field there): rays that left the box,
@@ -506,7 +516,7 @@ __device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const R
         o[(size_t)ln + lr] = (double)atanf((float)y[3 + p0] * (1.f / 299792458.f) / uc);
         o[(size_t)3 * ln + lr] = (double)atanf((float)y[3 + p1] * (1.f / 299792458.f) / uc);
     }
-    if (phase) phase[r] = (double)R.ph + (double)R.phc;
+    if (phase) phase[r] = ph64 ? ph_get(R) : (double)R.ph + (double)R.phc;
     if (status) status[r] = R.code;
     if (nsteps) nsteps[r] = R.nacc;
 }
@@ -567,7 +577,14 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     }
     float Hs[7][3];
     float q0;
-    stage_eval(G, nodes, K, R, coef, R.fr, Hs[0], q0);
+    {  // stage 0 is at the ray's own position, always inside the current cell's range
+        const float2 hab = tri2(coef[0], R.fr[0], R.fr[1], R.fr[2]);
+        const float2 hcq = tri2(coef[1], R.fr[0], R.fr[1], R.fr[2]);
+        Hs[0][0] = hab.x;
+        Hs[0][1] = hab.y;
+        Hs[0][2] = hcq.x;
+        q0 = K.with_phase ? hcq.y : 0.f;
+    }
     // Predict the first face crossing of the cell from position, velocity and
     // acceleration; aim the step end at it.  Leaving through a box face within
     // kBoxPath: the ray has left (the field beyond is the fill value 0).
@@ -576,15 +593,20 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     for (int a = 0; a < 3; ++a) {
         const float vel = G.r[a] * R.u[a];
         const float acc = G.r[a] * Hs[0][a];
-        const float hu = first_hit(vel, acc, 1.f - R.fr[a]);
-        const float hl = first_hit(-vel, -acc, R.fr[a]);
+        // the face ahead; the one behind only for a ray that turns back inside
+        // the cell (it cannot reach the face ahead): the same first crossing as
+        // testing both faces
+        const bool up = vel > 0.f || (vel == 0.f && acc > 0.f);
+        const float sv = up ? vel : -vel, sa = up ? acc : -acc;
+        float hit = first_hit(sv, sa, up ? 1.f - R.fr[a] : R.fr[a]);
+        if (hit == 3.0e38f && sa < 0.f) hit = first_hit(-sv, -sa, up ? R.fr[a] : 1.f - R.fr[a]);
         const bool box_up = R.ci[a] == G.n[a] - 2, box_lo = R.ci[a] == 0;
         if ((box_up && vel > 0.f && (1.f - R.fr[a]) <= kBoxPath * vel) ||
             (box_lo && vel < 0.f && R.fr[a] <= -kBoxPath * vel)) {
             R.state = 1;
             return;
         }
-        hf = fminf(hf, fminf(hu, hl));
+        hf = fminf(hf, hit);
     }
     ++R.natt;
     bool last = false;
@@ -658,16 +680,30 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     const float q0u = fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2]));
     const float q1u = fmaf(un[0], un[0], fmaf(un[1], un[1], un[2] * un[2]));
     const float inv_scu = rsqrtf(fmaxf(q0u, q1u)) * K.inv_rtol;  // 1 / (rtol |u|)
+    float eus[3], eps[3];
+    {  // the error sums of the transverse pair packed (lane-wise the scalar FMAs below)
+        float2 eu2 = make_float2(0.f, 0.f), ep2 = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 7; ++k) eu2 = __ffma2_rn(T.e2[k], make_float2(Hs[k][0], Hs[k][1]), eu2);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) ep2 = __ffma2_rn(T.ea2[k], make_float2(Hs[k][0], Hs[k][1]), ep2);
+        eus[0] = eu2.x;
+        eus[1] = eu2.y;
+        eps[0] = ep2.x;
+        eps[1] = ep2.y;
+        float eu = 0.f, ep = 0.f;
+#pragma unroll
+        for (int k = 0; k < 7; ++k) eu = fmaf(T.e[k], Hs[k][2], eu);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) ep = fmaf(T.ea[k], Hs[k][2], ep);
+        eus[2] = eu;
+        eps[2] = ep;
+    }
     float es = 0.f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        float eu = 0.f, ep = 0.f;
-#pragma unroll
-        for (int k = 0; k < 7; ++k) eu = fmaf(T.e[k], Hs[k][c], eu);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) ep = fmaf(T.ea[k], Hs[k][c], ep);
-        eu *= h;
-        ep *= h * h * G.r[c];
+        const float eu = eus[c] * h;
+        const float ep = eps[c] * (h * h * G.r[c]);
         const float x1 = eu * inv_scu;
         const float x2 = ep * K.inv_atol_cells;
         es = fmaf(x1, x1, fmaf(x2, x2, es));
@@ -676,8 +712,9 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     float dphi = 0.f;
     if (K.with_phase) {
         dphi = h * phb;
-        const float phn = R.ph + dphi;
-        const float scp = K.atol_phase + K.rtol * fmaxf(fabsf(R.ph), fabsf(phn));
+        const float phv = K.phase_f64 ? (float)ph_get(R) : R.ph;
+        const float phn = phv + dphi;
+        const float scp = K.atol_phase + K.rtol * fmaxf(fabsf(phv), fabsf(phn));
         const float x = __fdividef(h * phe, scp);
         es = fmaf(x, x, es);
         neq = 7;
@@ -739,7 +776,10 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         R.sigc = __fsub_rn(__fsub_rn(t, R.sig), y);
         R.sig = t;
     }
-    if (K.with_phase) neumaier(R.ph, R.phc, dphi);
+    if (K.with_phase) {
+        if (K.phase_f64) ph_set(R, ph_get(R) + (double)dphi);
+        else neumaier(R.ph, R.phc, dphi);
+    }
     if (renormalise(G, R)) R.state = 1;
     else if (last) R.state = 2;
 }
@@ -818,7 +858,8 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
                     nodes = src.nodes;
                     double P0[3], u0[3];
                     if (!init_ray(pol.geo(ray), src, s0, np, ray, R, P0, u0)) {
-                        finish_ray<false>(pol.geo(ray), src, R, P0, u0, ray, np, sf, rf, phase, status, nsteps);
+                        finish_ray<false>(pol.geo(ray), src, R, P0, u0, ray, np, sf, rf, phase, status, nsteps,
+                                          K.phase_f64 != 0);
                         busy = false;  // picked up again on the next pass
                     }
                 } else if (nb == ne) {
@@ -838,7 +879,7 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
             step(pol.geo(ray), pol.nodes(nodes), K, T, R, coef);
             if (R.state != 0) {
                 finish_ray<true>(pol.geo(ray), pol.src(ray), R, nullptr, nullptr, ray, np, sf, rf, phase, status,
-                                 nsteps);
+                                 nsteps, K.phase_f64 != 0);
                 busy = false;
             }
         }
@@ -1048,6 +1089,7 @@ int make_ctl(const tt_trace_opts* opts, Ctl* K)
     K->inv_atol_cells = (float)(1.0 / opts->atol);
     K->atol_phase = (float)(opts->with_phase ? opts->atol_phase : 1.0);
     K->with_phase = opts->with_phase ? 1 : 0;
+    K->phase_f64 = (opts->with_phase && opts->phase_f64) ? 1 : 0;
     K->max_steps = opts->max_steps > 0 ? opts->max_steps : TT_DEFAULT_MAX_STEPS;
     const int ch = opts->ray_chunk;
     if (ch != 0 && (ch < 32 || ch > 1024 || ch % 32)) return tt::invalid("trace_f32: ray_chunk must be 0 or 32..1024, a multiple of 32");

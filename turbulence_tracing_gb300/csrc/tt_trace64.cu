@@ -196,121 +196,140 @@ __device__ double initial_step64(const Cube64& C, const RKDev& T, const double* 
     return h;
 }
 
-// One ray through scipy's RungeKutta._step_impl loop (safety 0.9, factors in
-// [0.2, 10], RMS norm, step clipped to t_bound, TOO_SMALL below 10 spacings of
-// t).  NS stages per step plus the FSAL evaluation at the new point; DOP853
-// (DOP = true) takes scipy's combined E5/E3 error norm.
-template <int NS, bool DOP, int NEQ>
-__device__ int integrate64(const Cube64& C, const RKDev& T, double* y, double t_bound, double rtol, double atol,
-                           long long max_steps, int* nacc_out)
+// One ray through scipy's RungeKutta loop (safety 0.9, factors in [0.2, 10],
+// RMS norm, step clipped to t_bound, TOO_SMALL below 10 spacings of t), cut
+// into single attempts so that a warp's lanes can each carry their own ray:
+// attempt() makes one try of a step (scipy's rk_step + _estimate_error_norm +
+// the accept/reject decision of _step_impl) and keeps the loop state in Ray64.
+// NS stages per step plus the FSAL evaluation at the new point; every stage's
+// rates are kept for all NEQ components and combined in scipy's order
+// (y + (sum_j K[j] a[s][j]) h).  DOP853 (DOP = true) takes scipy's combined
+// E5/E3 error norm.
+template <int NS, int NEQ>
+struct Ray64 {
+    double y[NEQ];
+    double K[NS + 1][NEQ];  // K[0]: the rates at y (scipy's self.f)
+    double t, h_abs;
+    long long natt, nacc;
+    bool fresh;     // the next attempt starts a new step (scipy's _step_impl entry)
+    bool rejected;  // a try of the current step was rejected
+};
+
+enum { kAttemptMore = -1 };
+
+template <int NEQ>
+__device__ inline void rhs64(const Cube64& C, const double* y, double* f)
 {
-    double K[NS + 1][NEQ];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) f[i] = y[3 + i];
+    accel64<NEQ>(C, y, y + 3, f + 3);
+}
+
+// Start a ray: rates at y0 and scipy's initial step.  Returns false for a
+// non-finite start (status NaN).
+template <int NS, int NEQ>
+__device__ bool start64(const Cube64& C, const RKDev& T, Ray64<NS, NEQ>& R, double t_bound, double rtol, double atol)
+{
+    R.t = 0.0;
+    R.natt = R.nacc = 0;
+    R.fresh = true;
+    R.rejected = false;
     for (int i = 0; i < NEQ; ++i)
-        if (!isfinite(y[i])) { *nacc_out = 0; return TT_RAY_NAN; }
+        if (!isfinite(R.y[i])) return false;
+    rhs64<NEQ>(C, R.y, R.K[0]);
+    R.h_abs = initial_step64<NEQ>(C, T, R.y, R.K[0] + 3, t_bound, rtol, atol);
+    return true;
+}
+
+// One try of a step.  Returns kAttemptMore while the ray goes on, else its
+// final tt_ray_status (TT_RAY_OK once t reaches t_bound).
+template <int NS, bool DOP, int NEQ>
+__device__ int attempt64(const Cube64& C, const RKDev& T, Ray64<NS, NEQ>& R, double t_bound, double rtol,
+                         double atol, long long max_steps)
+{
+    if (R.t == t_bound) return TT_RAY_OK;
+    const double min_step = 10.0 * fabs(nextafter(R.t, CUDART_INF) - R.t);
+    if (R.fresh) {
+        if (R.h_abs < min_step) R.h_abs = min_step;
+        R.rejected = false;
+        R.fresh = false;
+    }
+    if (R.h_abs < min_step) return TT_RAY_STEP_TOO_SMALL;
+    if (R.natt >= max_steps) return TT_RAY_MAX_STEPS;
+    ++R.natt;
+    double h = R.h_abs;
+    double t_new = R.t + h;
+    if (t_new - t_bound > 0) t_new = t_bound;
+    h = t_new - R.t;
+    R.h_abs = fabs(h);
+    double yn[NEQ];
+    // stages 1..NS-1 and the new point (the B row) at s = NS
+#pragma unroll 1
+    for (int s = 1; s <= NS; ++s) {
+        const double* a = s < NS ? T.a[s] : T.b;
+        double ys[NEQ];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) K[0][i] = y[3 + i];
-    accel64<NEQ>(C, y, y + 3, &K[0][3]);
-    long long nacc = 0, natt = 0;
-    double h_abs = initial_step64<NEQ>(C, T, y, &K[0][3], t_bound, rtol, atol);
-    double t = 0.0;
-    int code = TT_RAY_OK;
-    if (t != t_bound) {
-        for (;;) {
-            const double min_step = 10.0 * fabs(nextafter(t, CUDART_INF) - t);
-            if (h_abs < min_step) h_abs = min_step;
-            bool rejected = false;
-            double t_new;
-            double yn[NEQ];
-            for (;;) {
-                if (h_abs < min_step) { code = TT_RAY_STEP_TOO_SMALL; break; }
-                if (natt >= max_steps) { code = TT_RAY_MAX_STEPS; break; }
-                ++natt;
-                double h = h_abs;
-                t_new = t + h;
-                if (t_new - t_bound > 0) t_new = t_bound;
-                h = t_new - t;
-                h_abs = fabs(h);
+        for (int i = 0; i < NEQ; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < s; ++j) acc += R.K[j][i] * a[j];
+            ys[i] = R.y[i] + acc * h;
+        }
+        if (s == NS) {
 #pragma unroll
-                for (int s = 1; s < NS; ++s) {
-                    double ys[6];
+            for (int i = 0; i < NEQ; ++i) yn[i] = ys[i];
+        }
+        rhs64<NEQ>(C, ys, R.K[s]);
+    }
+    double e5s = 0.0, e3s = 0.0;
 #pragma unroll
-                    for (int i = 0; i < 6; ++i) {
-                        double acc = 0.0;
-#pragma unroll
-                        for (int j = 0; j < s; ++j) acc += K[j][i] * T.a[s][j];
-                        ys[i] = y[i] + acc * h;
-                    }
-#pragma unroll
-                    for (int i = 0; i < 3; ++i) K[s][i] = ys[3 + i];
-                    accel64<NEQ>(C, ys, ys + 3, &K[s][3]);
-                }
-#pragma unroll
-                for (int i = 0; i < NEQ; ++i) {
-                    double acc = 0.0;
-#pragma unroll
-                    for (int j = 0; j < NS; ++j) acc += K[j][i] * T.b[j];
-                    yn[i] = y[i] + h * acc;
-                }
-#pragma unroll
-                for (int i = 0; i < 3; ++i) K[NS][i] = yn[3 + i];
-                accel64<NEQ>(C, yn, yn + 3, &K[NS][3]);
-                double e5s = 0.0, e3s = 0.0;
-#pragma unroll
-                for (int i = 0; i < NEQ; ++i) {
-                    const double ay = fabs(y[i]), an = fabs(yn[i]);
-                    const double sc = atol + (ay > an ? ay : an) * rtol;
-                    double acc = 0.0, acc3 = 0.0;
-#pragma unroll
-                    for (int j = 0; j <= NS; ++j) {
-                        acc += K[j][i] * T.e[j];
-                        if (DOP) acc3 += K[j][i] * T.e3[j];
-                    }
-                    if (DOP) {
-                        const double x5 = acc / sc, x3 = acc3 / sc;
-                        e5s += x5 * x5;
-                        e3s += x3 * x3;
-                    } else {
-                        const double e = acc * h / sc;
-                        e5s += e * e;
-                    }
-                }
-                double en;
-                if (DOP) {
-                    if (e5s == 0.0 && e3s == 0.0) en = 0.0;
-                    else en = fabs(h) * e5s / sqrt((e5s + 0.01 * e3s) * (double)NEQ);
-                } else {
-                    en = sqrt(e5s) / sqrt((double)NEQ);
-                }
-                if (en < 1.0) {
-                    double factor;
-                    if (en == 0.0) factor = 10.0;
-                    else {
-                        factor = 0.9 * pow(en, T.err_exp);
-                        if (!(factor < 10.0)) factor = 10.0;
-                    }
-                    if (rejected && !(factor < 1.0)) factor = 1.0;
-                    h_abs *= factor;
-                    break;
-                } else {
-                    double factor = 0.9 * pow(en, T.err_exp);
-                    if (!(factor > 0.2)) factor = 0.2;
-                    h_abs *= factor;
-                    rejected = true;
-                }
-            }
-            if (code != TT_RAY_OK) break;
-            ++nacc;
-            t = t_new;
-#pragma unroll
-            for (int i = 0; i < NEQ; ++i) {
-                y[i] = yn[i];
-                K[0][i] = K[NS][i];
-            }
-            if (t - t_bound >= 0) break;
+    for (int i = 0; i < NEQ; ++i) {
+        const double ay = fabs(R.y[i]), an = fabs(yn[i]);
+        const double sc = atol + (ay > an ? ay : an) * rtol;
+        double acc = 0.0, acc3 = 0.0;
+        for (int j = 0; j <= NS; ++j) {
+            acc += R.K[j][i] * T.e[j];
+            if (DOP) acc3 += R.K[j][i] * T.e3[j];
+        }
+        if (DOP) {
+            const double x5 = acc / sc, x3 = acc3 / sc;
+            e5s += x5 * x5;
+            e3s += x3 * x3;
+        } else {
+            const double e = acc * h / sc;
+            e5s += e * e;
         }
     }
-    *nacc_out = (int)(nacc > 0x7fffffff ? 0x7fffffff : nacc);
-    return code;
+    double en;
+    if (DOP) {
+        if (e5s == 0.0 && e3s == 0.0) en = 0.0;
+        else en = fabs(h) * e5s / sqrt((e5s + 0.01 * e3s) * (double)NEQ);
+    } else {
+        en = sqrt(e5s) / sqrt((double)NEQ);
+    }
+    if (en < 1.0) {
+        double factor;
+        if (en == 0.0) factor = 10.0;
+        else {
+            factor = 0.9 * pow(en, T.err_exp);
+            if (!(factor < 10.0)) factor = 10.0;
+        }
+        if (R.rejected && !(factor < 1.0)) factor = 1.0;
+        R.h_abs *= factor;
+        ++R.nacc;
+        R.t = t_new;
+#pragma unroll
+        for (int i = 0; i < NEQ; ++i) {
+            R.y[i] = yn[i];
+            R.K[0][i] = R.K[NS][i];
+        }
+        R.fresh = true;
+        return (R.t - t_bound >= 0) ? TT_RAY_OK : kAttemptMore;
+    }
+    double factor = 0.9 * pow(en, T.err_exp);
+    if (!(factor > 0.2)) factor = 0.2;
+    R.h_abs *= factor;
+    R.rejected = true;
+    return kAttemptMore;
 }
 
 // ray_at_exit, particle_tracker.py:333-380
@@ -338,42 +357,79 @@ __device__ inline void ray_at_exit64(const double* y, int axis, double extent, d
     }
 }
 
-// Resident blocks of 128 per SM the register budget of each instantiation is
-// sized for: 3 for RK23 / RK45 (168 registers with phase, no spill), 2 for
-// DOP853's 13 stored stages.
-template <int NS, int NEQ>
+// Persistent form: the grid fills the GPU, each warp owns a contiguous range
+// of rays, and a lane whose ray is done takes the next ray of its warp's range
+// (ballot + popc, no global atomics), so the lanes of a warp stay busy while
+// rays with short and long paths mix.  Each loop pass makes one attempt on
+// every busy lane.  Registers: 3 blocks of 128 per SM for RK23 / RK45, 2 for
+// DOP853.
+template <int NS>
 struct Occ64 {
     static constexpr int blocks = NS <= 6 ? 3 : 2;
 };
 
+template <int NS, int NEQ>
+__device__ inline void finish64(const Ray64<NS, NEQ>& R, int code, long long r, long long np, int axis, double extent,
+                                double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
+                                int* __restrict__ status, int* __restrict__ nsteps)
+{
+    if (sf) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) sf[(size_t)i * np + r] = R.y[i];
+    }
+    if (rf) {
+        double o[4];
+        ray_at_exit64(R.y, axis, extent, o);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) rf[(size_t)i * np + r] = o[i];
+    }
+    if (phase) phase[r] = NEQ == 7 ? R.y[NEQ - 1] : 0.0;
+    if (status) status[r] = code;
+    if (nsteps) nsteps[r] = (int)(R.nacc > 0x7fffffff ? 0x7fffffff : R.nacc);
+}
+
 template <int NS, bool DOP, int NEQ>
-__global__ void __launch_bounds__(128, Occ64<NS, NEQ>::blocks)
+__global__ void __launch_bounds__(128, Occ64<NS>::blocks)
 trace64_kernel(Cube64 C, const __grid_constant__ RKDev T, const double* __restrict__ s0, long long np,
                double t_end, int axis, double extent, double rtol, double atol, long long max_steps,
                double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
                int* __restrict__ status, int* __restrict__ nsteps)
 {
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < np;
-         r += (long long)gridDim.x * blockDim.x) {
-        double y[NEQ];
+    const unsigned lane = threadIdx.x & 31u;
+    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    const long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const long long per = (np + nwarps - 1) / nwarps;
+    const long long wbeg = w * per < np ? w * per : np;
+    const long long wend = wbeg + per < np ? wbeg + per : np;
+    long long next = wbeg;  // warp-uniform cursor into the warp's range
+    long long r = -1;
+    Ray64<NS, NEQ> R;
+    for (;;) {
+        const bool need = r < 0;
+        const unsigned mask = __ballot_sync(0xffffffffu, need);
+        if (mask) {
+            const unsigned rank = __popc(mask & ((1u << lane) - 1u));
+            if (need && next + rank < wend) {
+                r = next + rank;
 #pragma unroll
-        for (int i = 0; i < 6; ++i) y[i] = s0[(size_t)i * np + r];
-        if (NEQ == 7) y[NEQ - 1] = 0.0;
-        int nacc = 0;
-        const int code = integrate64<NS, DOP, NEQ>(C, T, y, t_end, rtol, atol, max_steps, &nacc);
-        if (sf) {
-#pragma unroll
-            for (int i = 0; i < 6; ++i) sf[(size_t)i * np + r] = y[i];
+                for (int i = 0; i < 6; ++i) R.y[i] = s0[(size_t)i * np + r];
+                if (NEQ == 7) R.y[NEQ - 1] = 0.0;
+                if (!start64<NS, NEQ>(C, T, R, t_end, rtol, atol)) {
+                    finish64<NS, NEQ>(R, TT_RAY_NAN, r, np, axis, extent, sf, rf, phase, status, nsteps);
+                    r = -1;  // refilled on the next pass
+                }
+            }
+            const long long got = next + __popc(mask);
+            next = got < wend ? got : wend;
         }
-        if (rf) {
-            double o[4];
-            ray_at_exit64(y, axis, extent, o);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) rf[(size_t)i * np + r] = o[i];
+        if (__ballot_sync(0xffffffffu, r >= 0 || next < wend) == 0u) break;
+        if (r >= 0) {
+            const int code = attempt64<NS, DOP, NEQ>(C, T, R, t_end, rtol, atol, max_steps);
+            if (code != kAttemptMore) {
+                finish64<NS, NEQ>(R, code, r, np, axis, extent, sf, rf, phase, status, nsteps);
+                r = -1;
+            }
         }
-        if (phase) phase[r] = NEQ == 7 ? y[NEQ - 1] : 0.0;
-        if (status) status[r] = code;
-        if (nsteps) nsteps[r] = nacc;
     }
 }
 
@@ -511,18 +567,29 @@ int make_rkdev(const tt_rk_tableau* t, RKDev* D)
     return TT_OK;
 }
 
+// Resident blocks of 128 on the whole GPU, capped by the rays (a warp per 32 rays).
+template <typename KernelT>
+int resident_grid(KernelT kernel, long long np)
+{
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, 128, 0) != cudaSuccess || b < 1) b = 1;
+    long long g = (long long)b * tt::sm_count();
+    const long long need = (np + 127) / 128;
+    if (g > need) g = need;
+    return (int)(g < 1 ? 1 : g);
+}
+
 template <int NS, bool DOP>
 void launch64(bool phase, const Cube64& C, const RKDev& T, const double* s0, long long np, double t_end, int axis,
               double extent, const tt_trace_opts* o, long long maxs, double* sf, double* rf, double* ph, int* st,
               int* ns, cudaStream_t s)
 {
-    const int block = 128;
     if (phase)
-        trace64_kernel<NS, DOP, 7><<<grid_size(np, block), block, 0, s>>>(C, T, s0, np, t_end, axis, extent, o->rtol,
-                                                                         o->atol, maxs, sf, rf, ph, st, ns);
+        trace64_kernel<NS, DOP, 7><<<resident_grid(trace64_kernel<NS, DOP, 7>, np), 128, 0, s>>>(
+            C, T, s0, np, t_end, axis, extent, o->rtol, o->atol, maxs, sf, rf, ph, st, ns);
     else
-        trace64_kernel<NS, DOP, 6><<<grid_size(np, block), block, 0, s>>>(C, T, s0, np, t_end, axis, extent, o->rtol,
-                                                                         o->atol, maxs, sf, rf, ph, st, ns);
+        trace64_kernel<NS, DOP, 6><<<resident_grid(trace64_kernel<NS, DOP, 6>, np), 128, 0, s>>>(
+            C, T, s0, np, t_end, axis, extent, o->rtol, o->atol, maxs, sf, rf, ph, st, ns);
 }
 
 int trace64(const double* dndx, const double* dndy, const double* dndz, const double* ne_nc, int nx, int ny, int nz,

@@ -37,12 +37,13 @@ import numpy as np  # noqa: E402
 METRIC = "ray-steps/s at 512^3, 1e7 rays (FP32 persistent tracer, phase on, <=1 urad vs FP64)"
 UNIT = "ray-steps/s"
 ALG_BYTES_PHASE = 768  # 6 stages x 8 corners x 4 components x 4 B per ray-step (phase needs ne_nc)
-# DRAM traffic of one trace32_kernel launch on the default workload, from one
-# one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum; the
-# command and figures are in profiles/trace32_grf512_1e7rays_dram.md).  Other
-# workloads scale it by accepted ray-steps, which is stated in the output.
-TRAFFIC_CAPTURE = {"workload": "grf512_1e+07rays_phase_3det1024", "read_bytes": 20.44e9, "write_bytes": 5.84e9,
-                   "ray_steps": 4225486610}
+# Counters of one trace32_kernel launch on the default workload from a one-pass
+# ncu capture of this build (command and figures in
+# profiles/trace32_grf512_1e7rays_counters.md): warp instructions issued and
+# DRAM bytes.  The bench line scales them by accepted ray-steps for other
+# workloads and says so.
+TRACE32_CAPTURE = {"workload": "grf512_1e+07rays_phase_3det1024", "ray_steps": 4225486610,
+                   "warp_inst": 196200854988, "dram_read_bytes": 20.46e9, "dram_write_bytes": 5.83e9}
 
 
 def parse():
@@ -79,6 +80,7 @@ def parse():
     ap.add_argument("--sur-epochs", type=int, default=15)
     ap.add_argument("--sur-batch", type=int, default=16, help="fields per chunk in the surrogate pipeline")
     ap.add_argument("--sur-time", type=int, default=96, help="fresh fields for timing the pipeline")
+    ap.add_argument("--sur-stride", type=int, default=1, help="node planes per march step (1 or 2)")
     ap.add_argument("--no-stress", action="store_true", help="skip the stress workload (1024^3, 1e8 rays)")
     ap.add_argument("--stress-n", type=int, default=1024)
     ap.add_argument("--stress-rays", type=float, default=1e8)
@@ -303,18 +305,9 @@ def run_ours(a):
 
     peak, peak_kind = peaks()
     trace_ms_avg = float(np.mean(trace_ms))
-    alg_bytes = ray_steps_step * ALG_BYTES_PHASE
-    roof = {"kernel": "tt_trace_f32 (ray bucketing + persistent trace32_kernel)", "bound": "hbm",
-            "achieved": alg_bytes / (trace_ms_avg / 1e3) / 1e9, "peak": peak, "peak_kind": peak_kind,
-            "unit": "GB/s", "traffic": traffic_per_launch(workload_config(a)["workload"], ray_steps_step),
-            "traffic_source": ("ncu capture of this workload"
-                               if workload_config(a)["workload"] == TRAFFIC_CAPTURE["workload"]
-                               else "ncu capture of %s scaled by ray-steps" % TRAFFIC_CAPTURE["workload"]),
-            "note": "algorithmic bytes = 768 B per ray-step (6 stages x 8 corners x 4 comps x 4 B); "
-                    "a face-clamped step reads one cell's 8 nodes once and rays bucketed by entry tile "
-                    "share them in L1/L2, so DRAM traffic is ~6 B per ray-step and frac > 1 is cache reuse"}
-    roof["frac"] = roof["achieved"] / peak
-    roof["dram_gbs"] = roof["traffic"] / (trace_ms_avg / 1e3) / 1e9
+    roof = trace_roofline(workload_config(a)["workload"], ray_steps_step, trace_ms_avg / 1e3, peak, peak_kind,
+                          torch.cuda.get_device_properties(dev).multi_processor_count,
+                          (clocks or {}).get("sm_mhz") or 2070.0)
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32", "data": "synthetic (seeded GRF density and Gaussian beam)",
@@ -350,14 +343,36 @@ def run_ours(a):
     return res if rank == 0 else None
 
 
-def traffic_per_launch(workload, ray_steps):
-    """DRAM bytes per trace launch: the ncu capture's, scaled by accepted
-    ray-steps when the workload differs from the captured one."""
-    cap = TRAFFIC_CAPTURE
-    b = cap["read_bytes"] + cap["write_bytes"]
-    if workload == cap["workload"] and ray_steps == cap["ray_steps"]:
-        return b
-    return b * ray_steps / cap["ray_steps"]
+def trace_roofline(workload, ray_steps, seconds, peak, peak_kind, sms, sm_mhz):
+    """Rooflines of the trace launch.  HBM gathers (the contract's figure):
+    768 algorithmic bytes per ray-step over the launch time, against the
+    measured copy bandwidth; a face-aimed step reads one cell's 8 nodes once for
+    all stages and rays bucketed by entry tile share them in L1/L2, so this
+    exceeds 1 and DRAM carries a few bytes per ray-step.  Issue: the warp
+    instructions per ray-step of the captured launch times the ray-steps per
+    second, against SMs x 4 schedulers x the SM clock sampled during the run --
+    the resource the kernel is bound by."""
+    cap = TRACE32_CAPTURE
+    same = workload == cap["workload"] and ray_steps == cap["ray_steps"]
+    scale = 1.0 if same else ray_steps / cap["ray_steps"]
+    traffic = (cap["dram_read_bytes"] + cap["dram_write_bytes"]) * scale
+    wipr = cap["warp_inst"] / cap["ray_steps"]
+    issue_slots = sms * 4 * sm_mhz * 1e6
+    roof = {"kernel": "tt_trace_f32 (ray bucketing + persistent trace32_kernel)", "bound": "hbm",
+            "achieved": ray_steps * ALG_BYTES_PHASE / seconds / 1e9, "peak": peak, "peak_kind": peak_kind,
+            "unit": "GB/s", "traffic": traffic,
+            "traffic_source": ("one-pass ncu capture of this workload (profiles/trace32_grf512_1e7rays_counters.md)"
+                               if same else "ncu capture of %s scaled by ray-steps" % cap["workload"]),
+            "dram_gbs": traffic / seconds / 1e9,
+            "issue": {"warp_inst_per_ray_step": wipr, "issue_slots_per_s": issue_slots, "sms": sms,
+                      "sm_mhz": sm_mhz, "achieved_warp_inst_per_s": wipr * ray_steps / seconds},
+            "note": "algorithmic bytes = 768 B per ray-step (6 stages x 8 corners x 4 comps x 4 B), served from "
+                    "L1/L2 (frac > 1 is cache reuse; DRAM is dram_gbs); the binding resource is instruction "
+                    "issue: issue_frac = warp instructions per ray-step x ray-steps/s / (SMs x 4 x SM clock)"}
+    roof["frac"] = roof["achieved"] / peak
+    roof["dram_frac"] = roof["dram_gbs"] / peak
+    roof["issue_frac"] = roof["issue"]["achieved_warp_inst_per_s"] / issue_slots
+    return roof
 
 
 def fp64_compare(a, core, ne, x, s0_host, t_end, ext, out32, rays_per_s32):
@@ -498,7 +513,7 @@ def surrogate_run(a):
     from turbulence_tracing_gb300 import core, fno, surrogate as SG
 
     S = a.sur_size
-    W = SG.Workload(S)
+    W = SG.Workload(S, plane_stride=a.sur_stride)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     X, Y, _, _, steps_tr = SG.build_dataset(W, SG.draw_fields(a.sur_train, seed=a.seed + 11))
@@ -540,7 +555,8 @@ def surrogate_run(a):
     f8 = [W.field(p_) for p_ in SG.draw_fields(8, seed=a.seed + 14)]
     mb = torch.empty((8, W.n_maps, S, S), dtype=torch.float32, device=W.dev)
     wsb = torch.empty(core.march_batched_workspace_bytes(8, f8[0].shape), dtype=torch.uint8, device=W.dev)
-    us_march_b = timed(lambda: core.march_maps_batched(f8, W.x, W.x, W.x, S, lwl=W.lwl, out=mb, ws=wsb), 10) / 8
+    us_march_b = timed(lambda: core.march_maps_batched(f8, W.x, W.x, W.x, S, lwl=W.lwl, out=mb, ws=wsb,
+                                                       plane_stride=W.plane_stride), 10) / 8
     del f8, mb, wsb
     us_maps = timed(lambda: W.maps(ne0, out=so), 20)
     C = 32
@@ -572,7 +588,8 @@ def surrogate_run(a):
     errs = [SG.rel_l2(p_, t_) for p_, t_ in zip(I_p, I_t)]
     acc = [e for e, f in zip(errs, fell) if not f]
     bt_dev = max(SG.rel_l2(b_, t_) for b_, t_ in zip(I_b, I_t))
-    return {"grid": S, "train_fields": a.sur_train, "test_fields": a.sur_test, "timed_fields": len(fields),
+    return {"grid": S, "march_plane_stride": W.plane_stride, "train_fields": a.sur_train, "test_fields": a.sur_test,
+            "timed_fields": len(fields),
             "epochs": a.sur_epochs,
             "data_s": t_data, "train_samples_per_s": sps, "loss_first_last": [hist[0], hist[-1]],
             "target_rms": target_rms,

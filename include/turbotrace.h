@@ -351,6 +351,18 @@ int tt_march_maps_batched(const void* const* ne, int nfields, int ne_dtype, int 
                           const double* y, const double* z, double lwl, double ne_max, int P, float* out,
                           void* workspace, size_t workspace_bytes, void* stream);
 
+/* tt_march_maps_batched stepping plane_stride (1 or 2) node planes per step:
+ * with 2, the marched rays take one kick-drift-kick step of 2 h_z per two
+ * planes (the fields sampled on the even planes, d/dz still from the
+ * neighbouring planes) and a last single step to an odd last plane -- half
+ * the march's work, and an answer that aliases the grid-scale gradient (the
+ * surrogate's network learns the correction).  The straight-line maps are
+ * unchanged (every plane). */
+int tt_march_maps_batched_stride(const void* const* ne, int nfields, int ne_dtype, int nx, int ny, int nz,
+                                 const double* x, const double* y, const double* z, double lwl, double ne_max,
+                                 int P, int plane_stride, float* out, void* workspace, size_t workspace_bytes,
+                                 void* stream);
+
 /* Geometric-optics shadowgram of a deflection map theta FP32 [2][P][P] (angles
  * of rays leaving the centres of a P x P pixel grid of pitch `pitch` m):
  * intensity [P][P] = 1 / max(|det(I + D grad theta)|, 1e-3) after a free drift

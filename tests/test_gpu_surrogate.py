@@ -31,12 +31,14 @@ def _maps_restated(ne, x, lwl, S):
     return -0.5 * (bil(gx) * w).sum(-1), -0.5 * (bil(gy) * w).sum(-1)
 
 
-def _march_restated(ne, x, lwl, P, y=None, z=None):
+def _march_restated(ne, x, lwl, P, y=None, z=None, stride=1):
     """The plane march in float64: q = min(ne/n_c, 1), numpy.gradient
     derivatives, bilinear on the node planes (zero outside the grid), and
     kick-drift-kick in z from plane to plane on the ray equation, the closing
     kick's slope-dependent term at the slope predicted with the previous
-    step's acceleration; trapezoid phase in ds.
+    step's acceleration; trapezoid phase in ds.  stride 2: steps of two
+    planes (fields on the even planes) and a last single step to an odd
+    last plane.
     Then the straight ray from the same pixel centre: trapezoid deflection
     integrals on the planes.  Uniform axes x, y, z (y and z default to x)."""
     y = x if y is None else y
@@ -75,8 +77,11 @@ def _march_restated(ne, x, lwl, P, y=None, z=None):
     tx, ty = np.zeros_like(u), np.zeros_like(u)
     ax, ay = accel(f, tx, ty, q0)
     e, phi = dphase(f, tx, ty), np.zeros_like(u)
-    for k in range(1, nz):
-        d = hz
+    ks = list(range(0, nz, stride))
+    if ks[-1] != nz - 1:
+        ks.append(nz - 1)
+    for kp, k in zip(ks[:-1], ks[1:]):
+        d = (k - kp) * hz
         tx, ty = tx + d / 2 * ax, ty + d / 2 * ay
         u, v = u + d / hx * tx, v + d / hy * ty
         f = sample(u, v, k)
@@ -138,6 +143,25 @@ def test_march_maps_match_restatement(cuda, n, P):
     assert np.abs(m[3:5] - st[0:2]).max() <= 1e-5 * scale
     # the rays bend: the march is not the straight-line answer
     assert np.abs(m[0] - st[0]).max() > 1e-2 * scale
+
+
+@pytest.mark.parametrize("n,P", [(64, 64), (33, 40)])
+def test_march_stride2_matches_restatement(cuda, n, P):
+    """plane_stride 2 (the surrogate's half-cost march): the staged kernel and
+    the plain kernel against the float64 restatement of the same two-plane
+    steps, an even and an odd number of planes."""
+    from turbulence_tracing_gb300 import core
+
+    ne, x = R.workload_density(n, 1e-3, -3.0, 0.25, 2e25, 7)
+    for PP in (P, n // 2):
+        m = core.march_maps(ne, x, x, x, PP, lwl=1064e-9, plane_stride=2).cpu().numpy()
+        ref = _march_restated(ne, x, 1064e-9, PP, stride=2)
+        for c in range(5):
+            scale = np.abs(ref[c]).max()
+            assert np.abs(m[c] - ref[c]).max() <= 2e-4 * scale, (PP, c, np.abs(m[c] - ref[c]).max() / scale)
+        one = core.march_maps(ne, x, x, x, PP, lwl=1064e-9).cpu().numpy()
+        assert np.array_equal(m[3:5], one[3:5])      # the straight-line half does not depend on the stride
+        assert np.abs(m[0:2] - one[0:2]).max() > 0    # the marched half does
 
 
 @pytest.mark.parametrize("n,P", [(2, 1), (2, 3), (3, 2), (3, 1), (4, 64)])

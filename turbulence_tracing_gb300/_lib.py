@@ -141,6 +141,9 @@ SIGNATURES = {
     "tt_march_maps_batched": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_int, c_int, c_int, c_double_p,
                                       c_double_p, c_double_p, ctypes.c_double, ctypes.c_double, c_int, c_void_p,
                                       c_void_p, c_size, c_void_p]),
+    "tt_march_maps_batched_stride": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_int, c_int, c_int,
+                                             c_double_p, c_double_p, c_double_p, ctypes.c_double, ctypes.c_double,
+                                             c_int, c_int, c_void_p, c_void_p, c_size, c_void_p]),
     "tt_march_maps": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_double_p, c_double_p, c_double_p,
                               ctypes.c_double, ctypes.c_double, c_int, c_void_p, c_void_p, c_size, c_void_p]),
     "tt_shadowgram": (c_int, [c_void_p, c_int, ctypes.c_double, ctypes.c_double, c_void_p, c_void_p, c_void_p]),

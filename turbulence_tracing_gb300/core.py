@@ -443,9 +443,10 @@ def march_batched_workspace_bytes(nfields, shape):
     return int(_lib.lib().tt_march_maps_batched_workspace_bytes(int(nfields), nx, ny, nz))
 
 
-def march_maps_batched(fields, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, ws=None):
+def march_maps_batched(fields, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, ws=None, plane_stride=1):
     """march_maps over a list of same-shape density tensors in one pass
-    (tt_march_maps_batched): (len(fields), 5, P, P) float32."""
+    (tt_march_maps_batched_stride): (len(fields), 5, P, P) float32.
+    plane_stride 2: one march step per two node planes (half the work)."""
     dev = require_cuda()
     nf = len(fields)
     if not (1 <= nf <= _lib.MAX_MARCH_FIELDS):
@@ -464,13 +465,14 @@ def march_maps_batched(fields, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, ws
         ws = torch.empty(need, dtype=torch.uint8, device=dev)
     ptrs = (ctypes.c_void_p * nf)(*[t.data_ptr() for t in ts])
     dp = ctypes.POINTER(ctypes.c_double)
-    check(L.tt_march_maps_batched(ptrs, nf, _dtype_code(ts[0]), nx, ny, nz, xa.ctypes.data_as(dp),
-                                  ya.ctypes.data_as(dp), za.ctypes.data_as(dp), float(lwl), float(ne_max), int(P),
-                                  _ptr(out), _ptr(ws), need, _stream()), "tt_march_maps_batched")
+    check(L.tt_march_maps_batched_stride(ptrs, nf, _dtype_code(ts[0]), nx, ny, nz, xa.ctypes.data_as(dp),
+                                         ya.ctypes.data_as(dp), za.ctypes.data_as(dp), float(lwl), float(ne_max),
+                                         int(P), int(plane_stride), _ptr(out), _ptr(ws), need, _stream()),
+          "tt_march_maps_batched_stride")
     return out
 
 
-def march_maps(ne, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, ws=None):
+def march_maps(ne, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, ws=None, plane_stride=1):
     """(5, P, P) float32 from one pass over the density (tt_march_maps): exit
     angles (x, y) and phase of the pixel-centre rays marched one node plane per
     step through the ray equation -- the coarse solution the surrogate
@@ -487,9 +489,16 @@ def march_maps(ne, x, y, z, P, lwl=1053e-9, ne_max=1.0, out=None, ws=None):
     if ws is None or ws.numel() < need:
         ws = torch.empty(need, dtype=torch.uint8, device=dev)
     dp = ctypes.POINTER(ctypes.c_double)
-    check(_lib.lib().tt_march_maps(_ptr(ne_t), _dtype_code(ne_t), nx, ny, nz, xa.ctypes.data_as(dp),
-                                   ya.ctypes.data_as(dp), za.ctypes.data_as(dp), float(lwl), float(ne_max), int(P),
-                                   _ptr(out), _ptr(ws), need, _stream()), "tt_march_maps")
+    if plane_stride == 1:
+        check(_lib.lib().tt_march_maps(_ptr(ne_t), _dtype_code(ne_t), nx, ny, nz, xa.ctypes.data_as(dp),
+                                       ya.ctypes.data_as(dp), za.ctypes.data_as(dp), float(lwl), float(ne_max),
+                                       int(P), _ptr(out), _ptr(ws), need, _stream()), "tt_march_maps")
+    else:
+        ptrs = (ctypes.c_void_p * 1)(ne_t.data_ptr())
+        check(_lib.lib().tt_march_maps_batched_stride(ptrs, 1, _dtype_code(ne_t), nx, ny, nz, xa.ctypes.data_as(dp),
+                                                      ya.ctypes.data_as(dp), za.ctypes.data_as(dp), float(lwl),
+                                                      float(ne_max), int(P), int(plane_stride), _ptr(out), _ptr(ws),
+                                                      need, _stream()), "tt_march_maps_batched_stride")
     return out
 
 

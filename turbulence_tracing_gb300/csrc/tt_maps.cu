@@ -512,7 +512,8 @@ __device__ __forceinline__ void march_write(const MarchRay& r, double k0, int n,
 
 // Any pixel grid: one thread per ray, fields read from the padded q through L1/L2.
 __global__ void __launch_bounds__(128) march_kernel(const float* __restrict__ ws, size_t ws_field, int nx, int ny,
-                                                    int nz, MarchConsts mc, double k0, int P, float* __restrict__ out)
+                                                    int nz, MarchConsts mc, double k0, int P, int stride,
+                                                    float* __restrict__ out)
 {
     const int n = P * P;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -523,8 +524,9 @@ __global__ void __launch_bounds__(128) march_kernel(const float* __restrict__ ws
     MarchRay r;
     r.u = (float)(((pi + 0.5) / P) * (nx - 1));
     r.v = (float)(((pj + 0.5) / P) * (ny - 1));
-    for (int k = 0; k < nz; ++k) {
-        if (k > 0) march_kick_drift(r, mc.hz, mc);
+    for (int k = 0, kp = 0; k < nz; kp = k, k = (k + stride < nz || k == nz - 1) ? k + stride : nz - 1) {
+        const float h = (float)(k - kp) * mc.hz;
+        if (k > 0) march_kick_drift(r, h, mc);
         int i, j;
         float fx, fy;
         PlaneSample s{0.f, 0.f, 0.f, 0.f};
@@ -532,7 +534,7 @@ __global__ void __launch_bounds__(128) march_kernel(const float* __restrict__ ws
         if (k == 0)
             march_start(r, s, mc);
         else
-            march_kick(r, mc.hz, s, mc);
+            march_kick(r, h, s, mc);
     }
     march_write(r, k0, n, p, out);
 }
@@ -577,6 +579,7 @@ __device__ __noinline__ PlaneSample sample_slow(const float* ring, bool staged, 
 // Pixel grids at least as fine as the node grid (a tile spans at most
 // kMarchRows x kMarchCols node cells).  Window coordinates are padded ones:
 // row R = x + 1, column C = y + kPadY.
+template <int STRIDE>
 __global__ void __launch_bounds__(kMarchThreads) march_staged_kernel(const float* __restrict__ ws, size_t ws_field,
                                                                      int nx, int ny, int nz, MarchConsts mc, double k0,
                                                                      int P, float* __restrict__ out)
@@ -647,20 +650,22 @@ __global__ void __launch_bounds__(kMarchThreads) march_staged_kernel(const float
         b = (R - R0) * kMarchRY + (C - C0);
     };
     relocate();
+    // one plane per step, or (STRIDE 2) every second plane and the last one
     const float hh = 0.5f * mc.hz, dxi = mc.hz * mc.ihx, dyi = mc.hz * mc.ihy;
+    const float h2 = 2.f * mc.hz, hh2 = 0.5f * h2, dxi2 = h2 * mc.ihx, dyi2 = h2 * mc.ihy;
     // Step to plane k, whose ring slot K = k mod kMarchRing is a compile-time
     // constant: inside the volume the stencil's three planes sit at fixed
     // offsets from the ray's window base, so its shared loads need no address
     // arithmetic.  The first and last planes (one-sided d/dz) and rays outside
     // the staged window take the out-of-line sampler.
-    auto step = [&](int k, auto slot) {
+    auto step = [&](int k, auto slot, bool wide) {
         constexpr int K = decltype(slot)::value;
         const bool first = K == 0 && k == 0;
         if (!first) {  // half kick, drift to plane k
-            r.tx = fmaf(hh, r.ax, r.tx);
-            r.ty = fmaf(hh, r.ay, r.ty);
-            fx = fmaf(dxi, r.tx, fx);
-            fy = fmaf(dyi, r.ty, fy);
+            r.tx = fmaf(wide ? hh2 : hh, r.ax, r.tx);
+            r.ty = fmaf(wide ? hh2 : hh, r.ay, r.ty);
+            fx = fmaf(wide ? dxi2 : dxi, r.tx, fx);
+            fy = fmaf(wide ? dyi2 : dyi, r.ty, fy);
             if (!(fx >= 0.f && fx < 1.f && fy >= 0.f && fy < 1.f)) relocate();
         }
         PlaneSample s{0.f, 0.f, 0.f, 0.f};
@@ -676,7 +681,7 @@ __global__ void __launch_bounds__(kMarchThreads) march_staged_kernel(const float
         if (first)
             march_start(r, s, mc);
         else
-            march_kick(r, mc.hz, s, mc);
+            march_kick(r, wide ? h2 : mc.hz, s, mc);
     };
     // planes pl and pl + 1 (those below nz) into ring slots S and S + 1, one group
     auto issue2 = [&](int pl, auto slot) {
@@ -704,8 +709,13 @@ __global__ void __launch_bounds__(kMarchThreads) march_staged_kernel(const float
         __syncthreads();
         issue2(k + 5, Slot<(K + 5) % kMarchRing>{});
         if (active) {
-            step(k, slot);
-            if (k + 1 < nz) step(k + 1, Slot<K + 1>{});
+            if (STRIDE == 1) {
+                step(k, slot, false);
+                if (k + 1 < nz) step(k + 1, Slot<K + 1>{}, false);
+            } else {  // k is even: a double step to plane k, a single one to a last odd plane
+                step(k, slot, k > 0);
+                if (k + 1 == nz - 1) step(k + 1, Slot<K + 1>{}, false);
+            }
         }
     };
     static_assert(kMarchRing == 8, "ring schedule below assumes 8 planes");
@@ -739,10 +749,12 @@ extern "C" size_t tt_march_maps_workspace_bytes(int nx, int ny, int nz)
     return tt_march_maps_batched_workspace_bytes(1, nx, ny, nz);
 }
 
-extern "C" int tt_march_maps_batched(const void* const* ne, int nfields, int ne_dtype, int nx, int ny, int nz,
-                                     const double* x, const double* y, const double* z, double lwl, double ne_max,
-                                     int P, float* out, void* workspace, size_t workspace_bytes, void* stream)
+extern "C" int tt_march_maps_batched_stride(const void* const* ne, int nfields, int ne_dtype, int nx, int ny, int nz,
+                                            const double* x, const double* y, const double* z, double lwl,
+                                            double ne_max, int P, int plane_stride, float* out, void* workspace,
+                                            size_t workspace_bytes, void* stream)
 {
+    if (plane_stride != 1 && plane_stride != 2) return tt::invalid("march_maps: plane_stride must be 1 or 2");
     if (!ne || !x || !y || !z || !out || !workspace) return tt::invalid("march_maps: NULL pointer");
     if (nfields < 1 || nfields > TT_MAX_MARCH_FIELDS) return tt::invalid("march_maps: 1..TT_MAX_MARCH_FIELDS fields");
     if (nx < 2 || ny < 2 || nz < 2 || P < 1 || (long long)P * P > 0x7fffffffLL / 5 || nx > 65535 || ny > 65535 * 32)
@@ -795,15 +807,31 @@ extern "C" int tt_march_maps_batched(const void* const* ne, int nfields, int ne_
     // staged tiles need a tile to span at most kMarchRows x kMarchCols node cells
     if ((long long)(nx - 1) <= P && (long long)(ny - 1) <= P) {
         const size_t smem = (size_t)kMarchRing * kMarchPlane * sizeof(float);
-        TT_TRY(tt::cuda_status(cudaFuncSetAttribute(march_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                    (int)smem),
-                               "march_maps attribute"));
         const dim3 grid((P + kMarchCols - 1) / kMarchCols, (P + kMarchRows - 1) / kMarchRows, nfields);
-        march_staged_kernel<<<grid, kMarchThreads, smem, s>>>(ws, wsf, nx, ny, nz, mc, k0, P, out);
+        if (plane_stride == 1) {
+            TT_TRY(tt::cuda_status(cudaFuncSetAttribute(march_staged_kernel<1>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                                   "march_maps attribute"));
+            march_staged_kernel<1><<<grid, kMarchThreads, smem, s>>>(ws, wsf, nx, ny, nz, mc, k0, P, out);
+        } else {
+            TT_TRY(tt::cuda_status(cudaFuncSetAttribute(march_staged_kernel<2>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                                   "march_maps attribute"));
+            march_staged_kernel<2><<<grid, kMarchThreads, smem, s>>>(ws, wsf, nx, ny, nz, mc, k0, P, out);
+        }
     } else {
-        march_kernel<<<dim3((n + 127) / 128, nfields), 128, 0, s>>>(ws, wsf, nx, ny, nz, mc, k0, P, out);
+        march_kernel<<<dim3((n + 127) / 128, nfields), 128, 0, s>>>(ws, wsf, nx, ny, nz, mc, k0, P, plane_stride,
+                                                                     out);
     }
     return tt::launch_status("march_maps");
+}
+
+extern "C" int tt_march_maps_batched(const void* const* ne, int nfields, int ne_dtype, int nx, int ny, int nz,
+                                     const double* x, const double* y, const double* z, double lwl, double ne_max,
+                                     int P, float* out, void* workspace, size_t workspace_bytes, void* stream)
+{
+    return tt_march_maps_batched_stride(ne, nfields, ne_dtype, nx, ny, nz, x, y, z, lwl, ne_max, P, 1, out, workspace,
+                                        workspace_bytes, stream);
 }
 
 extern "C" int tt_march_maps(const void* ne, int ne_dtype, int nx, int ny, int nz, const double* x, const double* y,

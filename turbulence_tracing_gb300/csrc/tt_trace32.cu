@@ -593,20 +593,15 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     for (int a = 0; a < 3; ++a) {
         const float vel = G.r[a] * R.u[a];
         const float acc = G.r[a] * Hs[0][a];
-        // the face ahead; the one behind only for a ray that turns back inside
-        // the cell (it cannot reach the face ahead): the same first crossing as
-        // testing both faces
-        const bool up = vel > 0.f || (vel == 0.f && acc > 0.f);
-        const float sv = up ? vel : -vel, sa = up ? acc : -acc;
-        float hit = first_hit(sv, sa, up ? 1.f - R.fr[a] : R.fr[a]);
-        if (hit == 3.0e38f && sa < 0.f) hit = first_hit(-sv, -sa, up ? R.fr[a] : 1.f - R.fr[a]);
+        const float hu = first_hit(vel, acc, 1.f - R.fr[a]);
+        const float hl = first_hit(-vel, -acc, R.fr[a]);
         const bool box_up = R.ci[a] == G.n[a] - 2, box_lo = R.ci[a] == 0;
         if ((box_up && vel > 0.f && (1.f - R.fr[a]) <= kBoxPath * vel) ||
             (box_lo && vel < 0.f && R.fr[a] <= -kBoxPath * vel)) {
             R.state = 1;
             return;
         }
-        hf = fminf(hf, hit);
+        hf = fminf(hf, fminf(hu, hl));
     }
     ++R.natt;
     bool last = false;
@@ -680,30 +675,16 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     const float q0u = fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2]));
     const float q1u = fmaf(un[0], un[0], fmaf(un[1], un[1], un[2] * un[2]));
     const float inv_scu = rsqrtf(fmaxf(q0u, q1u)) * K.inv_rtol;  // 1 / (rtol |u|)
-    float eus[3], eps[3];
-    {  // the error sums of the transverse pair packed (lane-wise the scalar FMAs below)
-        float2 eu2 = make_float2(0.f, 0.f), ep2 = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int k = 0; k < 7; ++k) eu2 = __ffma2_rn(T.e2[k], make_float2(Hs[k][0], Hs[k][1]), eu2);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) ep2 = __ffma2_rn(T.ea2[k], make_float2(Hs[k][0], Hs[k][1]), ep2);
-        eus[0] = eu2.x;
-        eus[1] = eu2.y;
-        eps[0] = ep2.x;
-        eps[1] = ep2.y;
-        float eu = 0.f, ep = 0.f;
-#pragma unroll
-        for (int k = 0; k < 7; ++k) eu = fmaf(T.e[k], Hs[k][2], eu);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) ep = fmaf(T.ea[k], Hs[k][2], ep);
-        eus[2] = eu;
-        eps[2] = ep;
-    }
     float es = 0.f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float eu = eus[c] * h;
-        const float ep = eps[c] * (h * h * G.r[c]);
+        float eu = 0.f, ep = 0.f;
+#pragma unroll
+        for (int k = 0; k < 7; ++k) eu = fmaf(T.e[k], Hs[k][c], eu);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) ep = fmaf(T.ea[k], Hs[k][c], ep);
+        eu *= h;
+        ep *= h * h * G.r[c];
         const float x1 = eu * inv_scu;
         const float x2 = ep * K.inv_atol_cells;
         es = fmaf(x1, x1, fmaf(x2, x2, es));

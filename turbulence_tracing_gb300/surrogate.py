@@ -63,9 +63,10 @@ N_MAPS = 5  # tt_march_maps: marched (theta_x, theta_y, phase), then straight (t
 class Workload:
     """Fields, straight-line and marched maps, exact traces and shadowgrams at one grid size."""
 
-    def __init__(self, S, L=2e-3, lwl=1064e-9, rtol=1e-7, contrast=0.2):
+    def __init__(self, S, L=2e-3, lwl=1064e-9, rtol=1e-7, contrast=0.2, plane_stride=1):
         self.dev = core.require_cuda()
         self.S, self.L, self.lwl, self.rtol, self.contrast = S, L, lwl, rtol, contrast
+        self.plane_stride = plane_stride  # node planes per march step (2: half the march's work)
         self.in_ch = IN_CHANNELS
         self.n_maps = N_MAPS
         self.x = np.linspace(-L / 2, L / 2, S)
@@ -95,7 +96,8 @@ class Workload:
         """Marched and straight-line maps from one pass (5, S, S)."""
         if self.march_ws is None:
             self.march_ws = torch.empty(core.march_workspace_bytes(ne.shape), dtype=torch.uint8, device=self.dev)
-        return core.march_maps(ne, self.x, self.x, self.x, self.S, lwl=self.lwl, out=out, ws=self.march_ws)
+        return core.march_maps(ne, self.x, self.x, self.x, self.S, lwl=self.lwl, out=out, ws=self.march_ws,
+                               plane_stride=self.plane_stride)
 
     def trace(self, ne):
         """Exact FP32 trace of the pixel-centre rays: (theta (2,S,S) f32, phase (S,S) f64, steps tensor)."""
@@ -367,7 +369,8 @@ class Pipeline:
         sl.D_host[:n] = torch.as_tensor(D, dtype=torch.float64)
         with torch.cuda.stream(self.s_march):
             sl.D.copy_(sl.D_host, non_blocking=True)
-            core.march_maps_batched(chunk, W.x, W.x, W.x, W.S, lwl=W.lwl, out=sl.mar[:n], ws=self.ws)
+            core.march_maps_batched(chunk, W.x, W.x, W.x, W.S, lwl=W.lwl, out=sl.mar[:n], ws=self.ws,
+                                    plane_stride=W.plane_stride)
             sl.marched.record()
         with torch.cuda.stream(self.s_net):
             self.s_net.wait_event(sl.marched)
@@ -599,7 +602,7 @@ def _main(argv=None):
 
     def one():
         nonlocal y
-        core.march_maps_batched(fields, W.x, W.x, W.x, a.size, lwl=W.lwl, out=out, ws=ws)
+        core.march_maps_batched(fields, W.x, W.x, W.x, a.size, lwl=W.lwl, out=out, ws=ws, plane_stride=W.plane_stride)
         encode_batch(out, a.size, X)
         y = net.forward(X, out=y)
 

@@ -70,16 +70,18 @@ int tt_calc_dndr(const void* ne, int ne_dtype, int nx, int ny, int nz,
                  void* workspace, size_t workspace_bytes, void* stream);
 
 /* tt_calc_dndr_noalloc -- no counterpart in the reference.  The same results
- * as tt_calc_dndr for callers that cannot allocate device memory (a host
- * whose allocator owns all device buffers, or work enqueued while a stream is
- * being captured into a CUDA graph, where cudaMalloc is not allowed).  It
- * allocates nothing: its scratch is a fixed 590 KB device array inside the
- * library, present on every GPU that loads it until the process exits, so
- * every axis is limited to 8192 nodes (TT_ERR_TOO_LARGE beyond).  The first
- * call on a device looks up that array's device address (no allocation);
- * make that first call before any stream capture.  All calls share the
- * array: calls whose work overlaps on the GPU (other streams, other threads)
- * race and must be serialised by the caller. */
+ * as tt_calc_dndr for callers that cannot allocate device memory: a host
+ * application whose memory manager owns every device buffer (a framework's
+ * caching allocator, or a fixed device pool handed out up front) and does not
+ * allow allocations behind its back.  It allocates nothing: its scratch is a
+ * fixed 590 KB device array inside the library, present on every GPU that
+ * loads it until the process exits, so every axis is limited to 8192 nodes
+ * (TT_ERR_TOO_LARGE beyond).  The first call on a device looks up that
+ * array's device address (no allocation) and keeps it for the device's
+ * context: make that first call before any stream capture, and do not reset
+ * the device after it.  All calls share the array: calls whose work overlaps
+ * on the GPU (other streams, other threads) race and must be serialised by
+ * the caller. */
 int tt_calc_dndr_noalloc(const void* ne, int ne_dtype, int nx, int ny, int nz,
                          const double* x, const double* y, const double* z,
                          double lwl, double ne_max,

@@ -1,6 +1,6 @@
 """tt_calc_dndr_noalloc: the allocation-free calc_dndr for callers that
-cannot allocate device memory (a host application whose allocator owns every
-device buffer, or code enqueuing work during CUDA-graph stream capture).
+cannot allocate device memory (a host application whose memory manager owns
+every device buffer and allows no allocation behind its back).
 
 Called through the C ABI and compared with tt_calc_dndr (which takes a caller
 workspace) on two calls in a row with different grids, so a stale table from

@@ -1,5 +1,7 @@
 // Status strings, error detail and device queries shared by every entry point.
 #include <stdarg.h>
+
+#include <atomic>
 #include <string.h>
 
 #include "tt_common.cuh"
@@ -18,13 +20,17 @@ void set_detail(const char* fmt, ...)
 
 int sm_count()
 {
-    static int cached[64] = {0};
+    // per-device cache; threads may race to fill an entry, all with the same value
+    static std::atomic<int> cached[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 1;
-    if (dev >= 0 && dev < 64 && cached[dev] > 0) return cached[dev];
+    if (dev >= 0 && dev < 64) {
+        const int c = cached[dev].load(std::memory_order_relaxed);
+        if (c > 0) return c;
+    }
     int n = 1;
     if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
-    if (dev >= 0 && dev < 64) cached[dev] = n;
+    if (dev >= 0 && dev < 64) cached[dev].store(n, std::memory_order_relaxed);
     return n;
 }
 

@@ -183,19 +183,16 @@ extern "C" int tt_calc_dndr(const void* ne, int ne_dtype, int nx, int ny, int nz
 // calc_dndr without any allocation.
 //
 // For callers that cannot allocate device memory for the workspace: a host
-// application whose allocator owns every device buffer and forbids other
-// allocations, or code that enqueues work while its stream is being captured
-// into a CUDA graph (cudaMalloc is not allowed during capture).  The
-// numpy.gradient coefficient tables then live in the fixed array below,
-// which every GPU that loads this library keeps until the process exits.
+// application whose memory manager owns every device buffer (a framework's
+// caching allocator or a fixed device pool handed out up front) and forbids
+// allocations behind its back.  The numpy.gradient coefficient tables then
+// live in the fixed array below, which every GPU that loads this library
+// keeps until the process exits.
 // ===========================================================================
 namespace {
 
 constexpr int kNoAllocMaxAxis = 8192;  // nodes per axis the fixed tables can hold
 constexpr size_t kNoAllocDoubles = 3 * (4 + 3 * (size_t)kNoAllocMaxAxis);  // 590 KB
-
-std::mutex g_noalloc_mutex;
-double* g_noalloc_tables[64] = {nullptr};  // device address of g_calc_dndr_tables, per device
 
 }  // namespace
 
@@ -203,8 +200,14 @@ static __device__ __align__(256) double g_calc_dndr_tables[kNoAllocDoubles];
 
 namespace {
 
+std::mutex g_noalloc_mutex;
+double* g_noalloc_tables[64] = {nullptr};  // device address of g_calc_dndr_tables, per device
+
 // Device address of the fixed tables on the current device, looked up once per
-// device (the host-side name of a __device__ array is not a device address).
+// device at that device's first call (the host-side name of a __device__ array
+// is not a device address; cudaGetSymbolAddress gives it, with the device
+// current, and allocates nothing).  The address belongs to the device's
+// context: a device reset after the first call is not supported.
 int noalloc_tables(double** out)
 {
     int dev = 0;

@@ -32,6 +32,8 @@
 #include <math.h>
 #include <stddef.h>
 
+#include <atomic>
+
 #include "tt_common.cuh"
 
 namespace {
@@ -1099,13 +1101,14 @@ WsLayout ws_layout(int nbins, long long np)
 template <typename KernelT>
 int occupancy_grid(KernelT kernel, int block, int slot)
 {
-    static int cache[9][64] = {{0}};
+    // per-(kernel, device) cache; threads may race to fill an entry, all with the same value
+    static std::atomic<int> cache[9][64];
     int dev = 0;
     cudaGetDevice(&dev);
-    int b = (dev >= 0 && dev < 64) ? cache[slot][dev] : 0;
+    int b = (dev >= 0 && dev < 64) ? cache[slot][dev].load(std::memory_order_relaxed) : 0;
     if (b <= 0) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, block, 0) != cudaSuccess || b < 1) b = 1;
-        if (dev >= 0 && dev < 64) cache[slot][dev] = b;
+        if (dev >= 0 && dev < 64) cache[slot][dev].store(b, std::memory_order_relaxed);
     }
     return b * tt::sm_count();
 }

@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--lwl", type=float, default=1064e-9)
     ap.add_argument("--det", type=int, default=1024)
     ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--block", type=int, default=0, help="FP32 tracer threads per block (0 = the library's 256)")
     ap.add_argument("--fp64-rays", type=int, default=1000000)
     ap.add_argument("--check-rays", type=int, default=20000)
     ap.add_argument("--cpu-rays", type=int, default=8000)
@@ -264,7 +265,8 @@ def run_ours(a):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
-        core.trace_f32(vol, s0, t_end, ext, rtol=1e-7, atol=1e-5, atol_phase=1e-5, phase=True, ws=wsp, out=out)
+        core.trace_f32(vol, s0, t_end, ext, rtol=1e-7, atol=1e-5, atol_phase=1e-5, phase=True, ws=wsp, out=out,
+                       block_size=a.block)
         if record:
             e1.record()
             tr_ev.append((e0, e1))

@@ -861,7 +861,11 @@ def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
         it.histogram(bin_scale=bins_scale, pix_x=det, pix_y=det, weights=cube.phase)
         return int(cube.nsteps.sum()), sh.H.sum() + ke.H.sum() + it.Hw.sum()
 
-    one()
+    # warm-up: the first steps allocate the device buffers and the pinned host
+    # staging buffers that later steps reuse (a solve's results alternate
+    # between two of them while the previous results are still referenced)
+    for _ in range(3):
+        one()
     torch.cuda.synchronize()
     # each step ends in host arrays, so steps are timed one by one; the median
     # step is reported (host-side copies on a shared machine vary run to run)

@@ -1,7 +1,7 @@
 """Generate golden fixtures by running the reference implementation itself.
 
 Run in a checkout where the reference repository is available:
-    python tests/golden/make_golden.py /root/reference [fixture names]
+    python tests/golden/make_golden.py <reference checkout> [fixture names]
 It imports particle_tracking/particle_tracker.py, ray_transfer_matrix.py
 (with a stub matplotlib, which the reference imports only for plotting) and
 gaussian_fields/turboGen.py + calculate_spectrum_3d.py, runs them on small
@@ -214,4 +214,6 @@ def main(root, only=None):
 
 if __name__ == "__main__":
     # python make_golden.py [reference root] [fixture names to (re)write ...]
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", only=set(sys.argv[2:]) or None)
+    if len(sys.argv) < 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout> [fixture names ...]")
+    main(sys.argv[1], only=set(sys.argv[2:]) or None)

@@ -43,7 +43,7 @@ ALG_BYTES_PHASE = 768  # 6 stages x 8 corners x 4 components x 4 B per ray-step 
 # DRAM bytes.  The bench line scales them by accepted ray-steps for other
 # workloads and says so.
 TRACE32_CAPTURE = {"workload": "grf512_1e+07rays_phase_3det1024", "ray_steps": 4225486610,
-                   "warp_inst": 196200854988, "dram_read_bytes": 20.46e9, "dram_write_bytes": 5.83e9}
+                   "warp_inst": 194081634571, "dram_read_bytes": 20.48e9, "dram_write_bytes": 5.84e9}
 
 
 def parse():
@@ -841,15 +841,19 @@ def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
 
     quiet = builtins.print
 
+    parts = []
+
     def one():
+        t0 = time.perf_counter()
         builtins.print = lambda *k, **kw: None
         try:
             cube.external_ne(ne_pinned)
             cube.calc_dndr(lwl=a.lwl)
             cube.s0 = pinned
-            rf = cube.solve(precision="fp32", phase=True)
+            rf = cube.solve(precision="fp32", phase=True)  # returns after its stream is synchronised
         finally:
             builtins.print = quiet
+        parts.append(time.perf_counter() - t0)
         sh = rtm.Shadowgraphy(rf, focal_plane=0, L=100.0, R=25.0, Lx=2 * ext_mm, Ly=2 * ext_mm)
         sh.solve()
         sh.histogram(bin_scale=bins_scale, pix_x=det, pix_y=det)
@@ -873,6 +877,7 @@ def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
     if dist:
         dist.barrier()
     times, tot = [], 0
+    del parts[:]
     for _ in range(k):
         t0 = time.perf_counter()
         rs, _chk = one()
@@ -886,6 +891,7 @@ def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
     d2h = Np * (4 + 1) * 8 + Np * 2 * 4 + 4 * det * det * 8  # rf, phase; status, steps; 3 H + 1 Hw (sf stays on the device until read)
     return {"value": units / sec, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "seconds_per_step": sec, "steps": k, "step_seconds": times, "timing": "median step",
+            "solve_seconds": parts,  # density in, volume build, rays in, trace, results out (the rest: diagnostics)
             "path": "ElectronCube.external_ne(host density) + calc_dndr + solve(precision='fp32', phase=True) "
                     "+ Shadowgraphy, Schlieren_KE, phase-weighted Shadowgraphy histograms (host arrays in and out)"}
 

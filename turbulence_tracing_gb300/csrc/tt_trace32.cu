@@ -634,7 +634,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
 #pragma unroll
             for (int k = 0; k < s && k < 6; ++k) {
                 const float2 hk = make_float2(Hs[k][0], Hs[k][1]);
-                sa = __ffma2_rn(T.a2[s][k], hk, sa);
+                if (!(s == 6 && k == 1)) sa = __ffma2_rn(T.a2[s][k], hk, sa);  // a[6][1] = b[1] = 0
                 saa = __ffma2_rn(T.aa2[s][k], hk, saa);
             }
             const float2 uu = __ffma2_rn(h2, sa, u2v);
@@ -649,7 +649,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
             float sa = 0.f, saa = 0.f;
 #pragma unroll
             for (int k = 0; k < s && k < 6; ++k) {
-                sa = fmaf(T.a[s][k], Hs[k][c], sa);
+                if (!(s == 6 && k == 1)) sa = fmaf(T.a[s][k], Hs[k][c], sa);  // a[6][1] = b[1] = 0
                 saa = fmaf(T.aa[s][k], Hs[k][c], saa);
             }
             us[c] = fmaf(h, sa, R.u[c]);
@@ -657,7 +657,9 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         }
         float q;
         stage_eval(G, nodes, K, R, coef, Ps, Hs[s], q);
-        if (K.with_phase) {
+        // Dormand-Prince's b and e weights of stage 1 are zero: its phase rate
+        // is not needed (the sums are unchanged: an FMA with weight 0 adds an exact 0)
+        if (K.with_phase && s != 1) {
             const float u2 = fmaf(us[0], us[0], fmaf(us[1], us[1], us[2] * us[2]));
             const float sp = u2 * rsqrtf(u2);
             const float dph = G.kappa * nm1f(q) * sp;
@@ -682,7 +684,8 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     for (int c = 0; c < 3; ++c) {
         float eu = 0.f, ep = 0.f;
 #pragma unroll
-        for (int k = 0; k < 7; ++k) eu = fmaf(T.e[k], Hs[k][c], eu);
+        for (int k = 0; k < 7; ++k)
+            if (k != 1) eu = fmaf(T.e[k], Hs[k][c], eu);  // e[1] = 0
 #pragma unroll
         for (int k = 0; k < 6; ++k) ep = fmaf(T.ea[k], Hs[k][c], ep);
         eu *= h;

@@ -59,6 +59,12 @@ struct Tab {
     float2 ea2[6];
 };
 
+// The step loop skips the terms whose Dormand-Prince weight is zero in exact
+// arithmetic: b[1] = e[1] = 0 (stage 1's rates enter neither the new state nor
+// the error estimate, so its phase rate is not formed), (A A)[s][k] = 0 for
+// k >= s - 1 (A is strictly lower triangular: a stage's position waits only
+// for the accelerations up to two stages back), (A A)[6][1] = (B A)[1] = 0 and
+// (E A)[1] = 0.
 Tab make_tab()
 {
     const double C[7] = {0.0, 1.0 / 5, 3.0 / 10, 4.0 / 5, 8.0 / 9, 1.0, 1.0};
@@ -635,7 +641,9 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
             for (int k = 0; k < s && k < 6; ++k) {
                 const float2 hk = make_float2(Hs[k][0], Hs[k][1]);
                 if (!(s == 6 && k == 1)) sa = __ffma2_rn(T.a2[s][k], hk, sa);  // a[6][1] = b[1] = 0
-                saa = __ffma2_rn(T.aa2[s][k], hk, saa);
+                // (A A)[s][k] = 0 for k >= s - 1 (A strictly lower triangular): a stage's
+                // position does not wait for the previous stage's acceleration
+                if (k + 1 < s && !(s == 6 && k == 1)) saa = __ffma2_rn(T.aa2[s][k], hk, saa);  // and (A A)[6][1] = 0
             }
             const float2 uu = __ffma2_rn(h2, sa, u2v);
             const float2 pp = __ffma2_rn(hr2, __ffma2_rn(T.cs2[s], u2v, __fmul2_rn(h2, saa)), fr2);
@@ -650,7 +658,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
 #pragma unroll
             for (int k = 0; k < s && k < 6; ++k) {
                 if (!(s == 6 && k == 1)) sa = fmaf(T.a[s][k], Hs[k][c], sa);  // a[6][1] = b[1] = 0
-                saa = fmaf(T.aa[s][k], Hs[k][c], saa);
+                if (k + 1 < s && !(s == 6 && k == 1)) saa = fmaf(T.aa[s][k], Hs[k][c], saa);  // zeros of A A
             }
             us[c] = fmaf(h, sa, R.u[c]);
             Ps[c] = fmaf(h * G.r[c], fmaf(T.cs[s], R.u[c], h * saa), R.fr[c]);
@@ -687,7 +695,8 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         for (int k = 0; k < 7; ++k)
             if (k != 1) eu = fmaf(T.e[k], Hs[k][c], eu);  // e[1] = 0
 #pragma unroll
-        for (int k = 0; k < 6; ++k) ep = fmaf(T.ea[k], Hs[k][c], ep);
+        for (int k = 0; k < 6; ++k)
+            if (k != 1) ep = fmaf(T.ea[k], Hs[k][c], ep);  // (E A)[1] = 0
         eu *= h;
         ep *= h * h * G.r[c];
         const float x1 = eu * inv_scu;

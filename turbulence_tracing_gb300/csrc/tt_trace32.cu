@@ -43,72 +43,71 @@ __device__ __host__ inline uint32_t spread3(uint32_t v)
     return (v & 1u) | ((v & 2u) << 1) | ((v & 4u) << 2);
 }
 
-struct Tab {
-    float cs[7];
-    float a[7][6];   // row 6 = b
-    float aa[7][6];  // (A A)[s][k]
-    float e[7];
-    float ea[6];     // sum_j e_j a[j][k] with a[6] = b
-    float b[6];
-    // the same coefficients duplicated into pairs, for packed FP32x2 FMAs on
-    // the two transverse components
-    float2 cs2[7];
-    float2 a2[7][6];
-    float2 aa2[7][6];
-    float2 e2[7];
-    float2 ea2[6];
-};
-
-// The step loop skips the terms whose Dormand-Prince weight is zero in exact
-// arithmetic: b[1] = e[1] = 0 (stage 1's rates enter neither the new state nor
-// the error estimate, so its phase rate is not formed), (A A)[s][k] = 0 for
-// k >= s - 1 (A is strictly lower triangular: a stage's position waits only
-// for the accelerations up to two stages back), (A A)[6][1] = (B A)[1] = 0 and
-// (E A)[1] = 0.
-Tab make_tab()
+// Dormand-Prince 5(4) (Dormand & Prince 1980; scipy's RK45 tableau) as
+// compile-time functions: after the stage loops unroll every coefficient is an
+// immediate operand (kernel-parameter constants cost the packed FP32x2 FMAs a
+// register move each; immediates measured 7% faster).  Row 6 of A is B.  The
+// step loop also uses the products AA = A A (stage positions from the stored
+// accelerations) and EA = E A (the position error), formed here in double and
+// rounded to float once, as the scalar tableau would be.
+//
+// The step loop skips the terms whose weight is zero in exact arithmetic:
+// b[1] = e[1] = 0 (stage 1's rates enter neither the new state nor the error
+// estimate, so its phase rate is not formed), AA[s][k] = 0 for k >= s - 1 (A
+// is strictly lower triangular: a stage's position waits only for the
+// accelerations up to two stages back), AA[6][1] = (B A)[1] = 0 and EA[1] = 0.
+__host__ __device__ constexpr double dp_a(int s, int k)
 {
-    const double C[7] = {0.0, 1.0 / 5, 3.0 / 10, 4.0 / 5, 8.0 / 9, 1.0, 1.0};
-    double A[7][6] = {{0}};
-    const double Ar[6][5] = {
-        {0, 0, 0, 0, 0},
-        {1.0 / 5, 0, 0, 0, 0},
-        {3.0 / 40, 9.0 / 40, 0, 0, 0},
-        {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0},
-        {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0},
-        {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656}};
-    const double B[6] = {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84};
-    const double E[7] = {-71.0 / 57600, 0, 71.0 / 16695, -71.0 / 1920, 17253.0 / 339200, -22.0 / 525, 1.0 / 40};
-    for (int s = 0; s < 6; ++s)
-        for (int k = 0; k < 5; ++k) A[s][k] = Ar[s][k];
-    for (int k = 0; k < 6; ++k) A[6][k] = B[k];
-    Tab t;
-    for (int s = 0; s < 7; ++s) {
-        t.cs[s] = (float)C[s];
-        t.e[s] = (float)E[s];
-        for (int k = 0; k < 6; ++k) {
-            t.a[s][k] = (float)A[s][k];
-            double acc = 0.0;
-            for (int j = 0; j < 6; ++j) acc += A[s][j] * A[j][k];
-            t.aa[s][k] = (float)acc;
-        }
-    }
-    for (int k = 0; k < 6; ++k) {
-        double acc = 0.0;
-        for (int j = 0; j < 7; ++j) acc += E[j] * A[j][k];
-        t.ea[k] = (float)acc;
-        t.b[k] = (float)B[k];
-    }
-    for (int s = 0; s < 7; ++s) {
-        t.cs2[s] = make_float2(t.cs[s], t.cs[s]);
-        t.e2[s] = make_float2(t.e[s], t.e[s]);
-        for (int k = 0; k < 6; ++k) {
-            t.a2[s][k] = make_float2(t.a[s][k], t.a[s][k]);
-            t.aa2[s][k] = make_float2(t.aa[s][k], t.aa[s][k]);
-        }
-    }
-    for (int k = 0; k < 6; ++k) t.ea2[k] = make_float2(t.ea[k], t.ea[k]);
-    return t;
+    return s == 1 ? (k == 0 ? 1.0 / 5 : 0.0)
+         : s == 2 ? (k == 0 ? 3.0 / 40 : k == 1 ? 9.0 / 40 : 0.0)
+         : s == 3 ? (k == 0 ? 44.0 / 45 : k == 1 ? -56.0 / 15 : k == 2 ? 32.0 / 9 : 0.0)
+         : s == 4 ? (k == 0 ? 19372.0 / 6561 : k == 1 ? -25360.0 / 2187 : k == 2 ? 64448.0 / 6561
+                   : k == 3 ? -212.0 / 729 : 0.0)
+         : s == 5 ? (k == 0 ? 9017.0 / 3168 : k == 1 ? -355.0 / 33 : k == 2 ? 46732.0 / 5247
+                   : k == 3 ? 49.0 / 176 : k == 4 ? -5103.0 / 18656 : 0.0)
+         : s == 6 ? (k == 0 ? 35.0 / 384 : k == 2 ? 500.0 / 1113 : k == 3 ? 125.0 / 192
+                   : k == 4 ? -2187.0 / 6784 : k == 5 ? 11.0 / 84 : 0.0)
+         : 0.0;
 }
+
+__host__ __device__ constexpr double dp_e(int k)
+{
+    return k == 0 ? -71.0 / 57600 : k == 2 ? 71.0 / 16695 : k == 3 ? -71.0 / 1920
+         : k == 4 ? 17253.0 / 339200 : k == 5 ? -22.0 / 525 : k == 6 ? 1.0 / 40 : 0.0;
+}
+
+__host__ __device__ constexpr double dp_c(int s)
+{
+    return s == 0 ? 0.0 : s == 1 ? 1.0 / 5 : s == 2 ? 3.0 / 10 : s == 3 ? 4.0 / 5 : s == 4 ? 8.0 / 9 : 1.0;
+}
+
+__host__ __device__ constexpr double dp_aa(int s, int k)
+{
+    double acc = 0.0;
+    for (int j = 0; j < 6; ++j) acc += dp_a(s, j) * dp_a(j, k);
+    return acc;
+}
+
+__host__ __device__ constexpr double dp_ea(int k)
+{
+    double acc = 0.0;
+    for (int j = 0; j < 7; ++j) acc += dp_e(j) * dp_a(j, k);
+    return acc;
+}
+
+// the float coefficients the step loop uses
+__host__ __device__ constexpr float fa(int s, int k) { return (float)dp_a(s, k); }
+__host__ __device__ constexpr float faa(int s, int k) { return (float)dp_aa(s, k); }
+__host__ __device__ constexpr float fc(int s) { return (float)dp_c(s); }
+__host__ __device__ constexpr float fe(int k) { return (float)dp_e(k); }
+__host__ __device__ constexpr float fea(int k) { return (float)dp_ea(k); }
+
+// exactly zero for k >= s - 1; AA[6][1] and EA[1] are zero in exact arithmetic
+// and within a few ulps of zero in double (the skipped FMA adds below 1e-15 of an
+// acceleration, far under FP32's rounding)
+static_assert(dp_aa(3, 2) == 0.0 && dp_aa(6, 5) == 0.0, "A A is zero for k >= s - 1");
+static_assert(dp_aa(6, 1) < 1e-15 && dp_aa(6, 1) > -1e-15 && dp_ea(1) < 1e-15 && dp_ea(1) > -1e-15,
+              "A A [6][1] and E A [1] vanish");
 
 // Resident tracer threads per SM the register budget is sized for (the
 // launch bounds give each thread 65536 / kThreadsPerSM registers).
@@ -560,7 +559,7 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restric
 }
 
 // One attempted step.  Returns with R updated.
-__device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, const Tab& T, Ray& R,
+__device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, Ray& R,
                                      float2 (*coef)[8])
 {
     if (R.cell_dirty) {
@@ -625,8 +624,8 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         const float u2 = fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2]));
         const float sp = u2 * rsqrtf(u2);
         const float dph = G.kappa * nm1f(q0) * sp;
-        phb = T.b[0] * dph;
-        phe = T.e[0] * dph;
+        phb = fa(6, 0) * dph;
+        phe = fe(0) * dph;
     }
     const float2 h2 = make_float2(h, h);
     const float2 hr2 = make_float2(h * G.r[0], h * G.r[1]);
@@ -640,13 +639,11 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
 #pragma unroll
             for (int k = 0; k < s && k < 6; ++k) {
                 const float2 hk = make_float2(Hs[k][0], Hs[k][1]);
-                if (!(s == 6 && k == 1)) sa = __ffma2_rn(T.a2[s][k], hk, sa);  // a[6][1] = b[1] = 0
-                // (A A)[s][k] = 0 for k >= s - 1 (A strictly lower triangular): a stage's
-                // position does not wait for the previous stage's acceleration
-                if (k + 1 < s && !(s == 6 && k == 1)) saa = __ffma2_rn(T.aa2[s][k], hk, saa);  // and (A A)[6][1] = 0
+                if (!(s == 6 && k == 1)) sa = __ffma2_rn(make_float2(fa(s, k), fa(s, k)), hk, sa);
+                if (k + 1 < s && !(s == 6 && k == 1)) saa = __ffma2_rn(make_float2(faa(s, k), faa(s, k)), hk, saa);
             }
             const float2 uu = __ffma2_rn(h2, sa, u2v);
-            const float2 pp = __ffma2_rn(hr2, __ffma2_rn(T.cs2[s], u2v, __fmul2_rn(h2, saa)), fr2);
+            const float2 pp = __ffma2_rn(hr2, __ffma2_rn(make_float2(fc(s), fc(s)), u2v, __fmul2_rn(h2, saa)), fr2);
             us[0] = uu.x;
             us[1] = uu.y;
             Ps[0] = pp.x;
@@ -657,11 +654,11 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
             float sa = 0.f, saa = 0.f;
 #pragma unroll
             for (int k = 0; k < s && k < 6; ++k) {
-                if (!(s == 6 && k == 1)) sa = fmaf(T.a[s][k], Hs[k][c], sa);  // a[6][1] = b[1] = 0
-                if (k + 1 < s && !(s == 6 && k == 1)) saa = fmaf(T.aa[s][k], Hs[k][c], saa);  // zeros of A A
+                if (!(s == 6 && k == 1)) sa = fmaf(fa(s, k), Hs[k][c], sa);
+                if (k + 1 < s && !(s == 6 && k == 1)) saa = fmaf(faa(s, k), Hs[k][c], saa);
             }
             us[c] = fmaf(h, sa, R.u[c]);
-            Ps[c] = fmaf(h * G.r[c], fmaf(T.cs[s], R.u[c], h * saa), R.fr[c]);
+            Ps[c] = fmaf(h * G.r[c], fmaf(fc(s), R.u[c], h * saa), R.fr[c]);
         }
         float q;
         stage_eval(G, nodes, K, R, coef, Ps, Hs[s], q);
@@ -671,8 +668,8 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
             const float u2 = fmaf(us[0], us[0], fmaf(us[1], us[1], us[2] * us[2]));
             const float sp = u2 * rsqrtf(u2);
             const float dph = G.kappa * nm1f(q) * sp;
-            if (s < 6) phb = fmaf(T.b[s], dph, phb);
-            phe = fmaf(T.e[s], dph, phe);
+            if (s < 6) phb = fmaf(fa(6, s), dph, phb);
+            phe = fmaf(fe(s), dph, phe);
         }
         if (s == 6) {
 #pragma unroll
@@ -693,10 +690,10 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         float eu = 0.f, ep = 0.f;
 #pragma unroll
         for (int k = 0; k < 7; ++k)
-            if (k != 1) eu = fmaf(T.e[k], Hs[k][c], eu);  // e[1] = 0
+            if (k != 1) eu = fmaf(fe(k), Hs[k][c], eu);  // e[1] = 0
 #pragma unroll
         for (int k = 0; k < 6; ++k)
-            if (k != 1) ep = fmaf(T.ea[k], Hs[k][c], ep);  // (E A)[1] = 0
+            if (k != 1) ep = fmaf(fea(k), Hs[k][c], ep);  // (E A)[1] = 0
         eu *= h;
         ep *= h * h * G.r[c];
         const float x1 = eu * inv_scu;
@@ -798,7 +795,7 @@ __device__ __forceinline__ int instance_of(const Geo* g, int n, long long r)
 // is asked once per fetched ray; the node pointer is kept for the ray's steps
 // unless the policy has it as a constant (pol.nodes).
 template <typename Policy>
-__device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const Tab& T, const double* __restrict__ s0,
+__device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const double* __restrict__ s0,
                                                 long long np, const unsigned* __restrict__ perm,
                                                 unsigned long long* __restrict__ counter, double* __restrict__ sf,
                                                 double* __restrict__ rf, double* __restrict__ phase,
@@ -871,7 +868,7 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
         }
         if (__ballot_sync(0xffffffffu, busy || (!drained)) == 0u) break;
         if (busy) {
-            step(pol.geo(ray), pol.nodes(nodes), K, T, R, coef);
+            step(pol.geo(ray), pol.nodes(nodes), K, R, coef);
             if (R.state != 0) {
                 finish_ray<true>(pol.geo(ray), pol.src(ray), R, nullptr, nullptr, ray, np, sf, rf, phase, status,
                                  nsteps, K.phase_f64 != 0);
@@ -890,12 +887,12 @@ struct SinglePolicy {
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
-trace32_kernel(const Geo G, Ctl K, Tab T, const double* __restrict__ s0, long long np,
+trace32_kernel(const Geo G, Ctl K, const double* __restrict__ s0, long long np,
                const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
                double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
                int* __restrict__ status, int* __restrict__ nsteps)
 {
-    persistent_loop(SinglePolicy{&G}, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps);
+    persistent_loop(SinglePolicy{&G}, K, s0, np, perm, counter, sf, rf, phase, status, nsteps);
 }
 
 // Volumes of different shapes: each lane reads its ray's instance entry from
@@ -927,12 +924,12 @@ struct MixedPolicy {
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
-trace32_batched_kernel(const __grid_constant__ GeoTable table, Ctl K, Tab T, const double* __restrict__ s0, long long np,
+trace32_batched_kernel(const __grid_constant__ GeoTable table, Ctl K, const double* __restrict__ s0, long long np,
                        const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
                        double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
                        int* __restrict__ status, int* __restrict__ nsteps)
 {
-    persistent_loop(MixedPolicy{table.g, table.n, -1, table.g}, K, T, s0, np, perm, counter, sf, rf, phase, status,
+    persistent_loop(MixedPolicy{table.g, table.n, -1, table.g}, K, s0, np, perm, counter, sf, rf, phase, status,
                     nsteps);
 }
 
@@ -955,12 +952,12 @@ struct UniformPolicy {
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
-trace32_uniform_kernel(const __grid_constant__ GeoTable table, Ctl K, Tab T, const double* __restrict__ s0,
+trace32_uniform_kernel(const __grid_constant__ GeoTable table, Ctl K, const double* __restrict__ s0,
                        long long np, const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
                        double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
                        int* __restrict__ status, int* __restrict__ nsteps)
 {
-    persistent_loop(UniformPolicy{table.g, table.n}, K, T, s0, np, perm, counter, sf, rf, phase, status, nsteps);
+    persistent_loop(UniformPolicy{table.g, table.n}, K, s0, np, perm, counter, sf, rf, phase, status, nsteps);
 }
 
 // --- ray bucketing by (instance, entry tile) ----------------------------------
@@ -1125,11 +1122,6 @@ int occupancy_grid(KernelT kernel, int block, int slot)
     return b * tt::sm_count();
 }
 
-const Tab& tableau()
-{
-    static const Tab T = make_tab();
-    return T;
-}
 
 int bin_grid(long long np)
 {
@@ -1178,17 +1170,16 @@ int run(const GeoTable& table, int nbins, const Ctl& K, int block, const double*
     bin_scan_kernel<<<1, 1024, 0, s>>>(cnt, nbins);
     bin_scatter_kernel<<<bin_grid(np), 256, 0, s>>>(table, s0, np, cnt, perm);
     TT_TRY(tt::launch_status("trace_f32 ray binning"));
-    const Tab& T = tableau();
     const Ctl& Kc = K;
 #define TT_LAUNCH_SINGLE(BS, SLOT)                                                                    \
     trace32_kernel<BS><<<occupancy_grid(trace32_kernel<BS>, BS, SLOT), BS, 0, s>>>(                  \
-        table.g[0], Kc, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
+        table.g[0], Kc, s0, np, perm, counter, sf, rf, phase, status, nsteps)
 #define TT_LAUNCH_BATCH(BS, SLOT)                                                                     \
     trace32_batched_kernel<BS><<<occupancy_grid(trace32_batched_kernel<BS>, BS, SLOT), BS, 0, s>>>(  \
-        table, Kc, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
+        table, Kc, s0, np, perm, counter, sf, rf, phase, status, nsteps)
 #define TT_LAUNCH_UNIFORM(BS, SLOT)                                                                   \
     trace32_uniform_kernel<BS><<<occupancy_grid(trace32_uniform_kernel<BS>, BS, SLOT), BS, 0, s>>>(  \
-        table, Kc, T, s0, np, perm, counter, sf, rf, phase, status, nsteps)
+        table, Kc, s0, np, perm, counter, sf, rf, phase, status, nsteps)
     // block 0 = 256 (measured fastest on the 256^3 and 512^3 workloads)
     if (table.n == 1) {
         if (block == 64) TT_LAUNCH_SINGLE(64, 0);

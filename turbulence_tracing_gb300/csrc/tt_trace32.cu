@@ -228,11 +228,36 @@ __device__ __forceinline__ void load_cell(const Geo& G, const float4* __restrict
     poly2(hi2(n000), hi2(n001), hi2(n010), hi2(n011), hi2(n100), hi2(n101), hi2(n110), hi2(n111), coef[1]);
 }
 
+// Square roots and reciprocals of the phase rate and the face prediction as the
+// hardware's approximate instructions (sqrt.approx, rcp.approx: about 2^-22
+// relative, the same class as rsqrtf and __fdividef, with fewer instructions
+// around them; 8% faster together).
+__device__ __forceinline__ float sqrt_apx(float x)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rcp_apx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 __device__ __forceinline__ float nm1f(float q)
 {
-    float r = 1.0f - q;
-    r = r > 0.0f ? r : 0.0f;
-    return -__fdividef(q, 1.0f + r * rsqrtf(fmaxf(r, 1e-30f)));  // 2-ulp divide, ~1-ulp sqrt
+    const float r = 1.0f - q;
+    return -q * rcp_apx(1.0f + sqrt_apx(r > 0.0f ? r : 0.0f));
+}
+
+// Smallest h > 0 with v h + acc h^2 / 2 = d (d >= 0, moving from 0 toward d).
+__device__ __forceinline__ float first_hit(float v, float acc, float d)
+{
+    if (!(d > 0.f)) return 3.0e38f;
+    const float disc = fmaf(v, v, 2.f * acc * d);
+    if (disc < 0.f) return 3.0e38f;
+    const float den = v + sqrt_apx(disc);  // predictor only: approximate is fine
+    return den > 0.f ? 2.f * d * rcp_apx(den) : 3.0e38f;
 }
 
 // Neumaier summation s + x with running compensation c (no contraction).
@@ -283,15 +308,6 @@ constexpr float kTolE = 1e-3f;
 constexpr float kFacePath = 1e-3f;
 constexpr float kBoxPath = 1e-6f;
 
-// Smallest h > 0 with v h + acc h^2 / 2 = d (d >= 0, moving from 0 toward d).
-__device__ __forceinline__ float first_hit(float v, float acc, float d)
-{
-    if (!(d > 0.f)) return 3.0e38f;
-    const float disc = fmaf(v, v, 2.f * acc * d);
-    if (disc < 0.f) return 3.0e38f;
-    const float den = v + disc * rsqrtf(fmaxf(disc, 1e-30f));  // predictor only: approximate is fine
-    return den > 0.f ? __fdividef(2.f * d, den) : 3.0e38f;
-}
 
 // Exact lookup (RegularGridInterpolator semantics, fill 0 outside) at cell
 // ci + floor(P), used when a stage leaves the current cell.  Scalars in,
@@ -622,7 +638,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     float Pn[3], un[3];
     if (K.with_phase) {
         const float u2 = fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2]));
-        const float sp = u2 * rsqrtf(u2);
+        const float sp = sqrt_apx(u2);
         const float dph = G.kappa * nm1f(q0) * sp;
         phb = fa(6, 0) * dph;
         phe = fe(0) * dph;
@@ -666,7 +682,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         // is not needed (the sums are unchanged: an FMA with weight 0 adds an exact 0)
         if (K.with_phase && s != 1) {
             const float u2 = fmaf(us[0], us[0], fmaf(us[1], us[1], us[2] * us[2]));
-            const float sp = u2 * rsqrtf(u2);
+            const float sp = sqrt_apx(u2);
             const float dph = G.kappa * nm1f(q) * sp;
             if (s < 6) phb = fmaf(fa(6, s), dph, phb);
             phe = fmaf(fe(s), dph, phe);
@@ -684,18 +700,30 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     const float q0u = fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2]));
     const float q1u = fmaf(un[0], un[0], fmaf(un[1], un[1], un[2] * un[2]));
     const float inv_scu = rsqrtf(fmaxf(q0u, q1u)) * K.inv_rtol;  // 1 / (rtol |u|)
-    float es = 0.f;
+    float eus[3], eps[3];
+    {  // the error sums of the transverse pair packed (lane-wise the scalar FMAs)
+        float2 eu2 = make_float2(0.f, 0.f), ep2 = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
+        for (int k = 0; k < 7; ++k)
+            if (k != 1) eu2 = __ffma2_rn(make_float2(fe(k), fe(k)), make_float2(Hs[k][0], Hs[k][1]), eu2);
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+            if (k != 1) ep2 = __ffma2_rn(make_float2(fea(k), fea(k)), make_float2(Hs[k][0], Hs[k][1]), ep2);
+        eus[0] = eu2.x; eus[1] = eu2.y; eps[0] = ep2.x; eps[1] = ep2.y;
         float eu = 0.f, ep = 0.f;
 #pragma unroll
         for (int k = 0; k < 7; ++k)
-            if (k != 1) eu = fmaf(fe(k), Hs[k][c], eu);  // e[1] = 0
+            if (k != 1) eu = fmaf(fe(k), Hs[k][2], eu);
 #pragma unroll
         for (int k = 0; k < 6; ++k)
-            if (k != 1) ep = fmaf(fea(k), Hs[k][c], ep);  // (E A)[1] = 0
-        eu *= h;
-        ep *= h * h * G.r[c];
+            if (k != 1) ep = fmaf(fea(k), Hs[k][2], ep);
+        eus[2] = eu; eps[2] = ep;
+    }
+    float es = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float eu = eus[c] * h;
+        const float ep = eps[c] * (h * h * G.r[c]);
         const float x1 = eu * inv_scu;
         const float x2 = ep * K.inv_atol_cells;
         es = fmaf(x1, x1, fmaf(x2, x2, es));

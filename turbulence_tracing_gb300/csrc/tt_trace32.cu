@@ -735,11 +735,11 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         const float phv = K.phase_f64 ? (float)ph_get(R) : R.ph;
         const float phn = phv + dphi;
         const float scp = K.atol_phase + K.rtol * fmaxf(fabsf(phv), fabsf(phn));
-        const float x = h * phe * rcp_apx(scp);
+        const float x = __fdividef(h * phe, scp);
         es = fmaf(x, x, es);
         neq = 7;
     }
-    const float en = sqrt_apx(es * (neq == 7 ? (1.f / 7.f) : (1.f / 6.f)));
+    const float en = sqrtf(es * (neq == 7 ? (1.f / 7.f) : (1.f / 6.f)));
     if (!(en == en)) {
         R.code = TT_RAY_NAN;
         R.state = 3;
@@ -764,10 +764,10 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         float over = 0.f;  // path past the crossed face
         bool box = false;
         if (Pn[a] > 1.f && R.fr[a] <= 1.f) {
-            over = (Pn[a] - 1.f) * rcp_apx(fmaxf(vend, 1e-6f));
+            over = __fdividef(Pn[a] - 1.f, fmaxf(vend, 1e-6f));
             box = R.ci[a] == G.n[a] - 2;
         } else if (Pn[a] < 0.f && R.fr[a] >= 0.f) {
-            over = -Pn[a] * rcp_apx(fmaxf(-vend, 1e-6f));
+            over = __fdividef(-Pn[a], fmaxf(-vend, 1e-6f));
             box = R.ci[a] == 0;
         }
         if (over > (box ? kBoxPath : kFacePath)) {

@@ -447,11 +447,13 @@ def batched_run(a):
     [0.05, 0.3], background 1e23..1e25 m^-3, 1e5..4e6 rays log-uniform,
     sigma 0.25 L, 0.05 mrad, L = 2 mm, 512^2 shadowgram each).  Pipeline per
     step, one CUDA graph: volume builds, ray bucketing, the persistent trace
-    launches, shadowgrams.  The ensemble's set-up times the launch modes on
-    the ensemble itself (one batched launch per grid shape, or one launch per
-    instance) and keeps the faster; the single mixed-shape launch and the
-    eager one-launch-per-instance form are timed beside it.  The same is
-    repeated for small instances (2e3..8e4 rays)."""
+    launches, shadowgrams.  The ensemble's set-up times the launch forms on
+    the ensemble itself (one mixed-shape launch for all instances, one
+    batched launch per grid shape, or one launch per instance), each with
+    every idle lane refilled at once and with a warp's 32 lanes refilled
+    together, and keeps the fastest; the eager one-launch-per-instance form
+    with the tracer's defaults is timed beside it.  The same is repeated for
+    small instances (2e3..8e4 rays)."""
     import torch
 
     from turbulence_tracing_gb300 import ensemble
@@ -476,14 +478,14 @@ def batched_run(a):
         bad = int((E.out["status"] != 0).sum().item())
         chosen = E.mode
         trace_ms = {m: E.mode_ms[m] for m in E.mode_ms}
-        E.mode = "one_launch"
-        trace_ms["one_launch"] = timed(E._trace_only, 2)
-        E.mode = chosen
+        best = {m: min(v for k, v in trace_ms.items() if k.startswith(m + "/"))
+                for m in ("one_launch", "grouped", "per_instance")}
         ms_eager = timed(E.run_unbatched, 1)
         r = {"instances": len(inst), "rays": E.ntot, "ray_steps_per_step": steps, "mode": chosen,
+             "refill_lanes": E.refill, "one_launch_over_per_instance": best["one_launch"] / best["per_instance"],
              "launches": len(E._launches()), "block_size": E.block, "graph_ms_per_step": ms,
              "ray_steps_per_s": steps / (ms / 1e3), "rays_per_s": E.ntot / (ms / 1e3), "non_ok_rays": bad,
-             "trace_only_ms_by_mode": trace_ms, "eager_one_launch_per_instance_ms_per_step": ms_eager,
+             "trace_only_ms_by_mode_refill": trace_ms, "eager_one_launch_per_instance_ms_per_step": ms_eager,
              "speedup_vs_eager_per_instance": ms_eager / ms}
         sizes = {}
         for p in inst:

@@ -78,6 +78,28 @@ def test_volume_plan_geometry():
         core.volume_plan((10, 10, 10), np.cumsum(np.arange(1, 11.0)), x[:10], x[:10], 2, 1064e-9)
 
 
+def test_trace_f32_options_checked_before_any_launch():
+    """tt_trace_opts is validated before the FP32 tracer touches the device
+    (with np = 0 the call returns right after the checks)."""
+    from turbulence_tracing_gb300 import _lib, core
+
+    L = _lib.lib()
+    x = np.linspace(-1e-3, 1e-3, 40)
+    v = core.volume_plan((40, 40, 40), x, x, x, 2, 1064e-9)
+    v.nodes = ctypes.c_void_p(256)  # never dereferenced: no ray is traced
+    for refill, want in ((0, 0), (1, 0), (32, 0), (33, 1), (-1, 1)):
+        o = core._opts(1e-7, 1e-5, 1e-5, None, True, refill_lanes=refill)
+        assert L.tt_trace_f32(ctypes.byref(v), None, 0, 1e-11, 1e-3, ctypes.byref(o), None, None, None, None, None,
+                              None, 0, None) == want, refill
+    assert b"refill_lanes" in L.tt_last_error_detail()
+    o = core._opts(1e-7, 1e-5, 1e-5, None, True, block_size=96)
+    assert L.tt_trace_f32(ctypes.byref(v), None, 0, 1e-11, 1e-3, ctypes.byref(o), None, None, None, None, None,
+                          None, 0, None) == 1
+    o = core._opts(1e-7, 1e-5, 1e-5, None, True, ray_chunk=48)
+    assert L.tt_trace_f32(ctypes.byref(v), None, 0, 1e-11, 1e-3, ctypes.byref(o), None, None, None, None, None,
+                          None, 0, None) == 1
+
+
 def test_no_gpu_means_loud_failure():
     import torch
 

@@ -75,6 +75,31 @@ def test_brick_depth_and_block_size_do_not_change_results(cuda):
                 assert all(torch.equal(a, b) for a, b in zip(got, ref)), (bd, block)
 
 
+def test_refill_lanes_do_not_change_results(cuda):
+    """A warp refilled lane by lane (refill_lanes 1) or 32 lanes at a time
+    carries each ray through the same arithmetic: single and batched launches
+    agree bit for bit."""
+    from turbulence_tracing_gb300 import core
+
+    ne, x = R.workload_density(36, 1e-3, -5 / 3, 0.2, 5e24, 4)
+    s0 = R.gaussian_beam(3000, 0.25e-3, 1e-3, x.max(), np.random.default_rng(5))
+    t_end = R.t_end(x.max())
+    vol = core.build_volume(ne, x, x, x, 2, lwl=LWL)
+    ref = core.trace_f32(vol, s0, t_end, x.max(), phase=True)
+    for rl in (8, 32):
+        o = core.trace_f32(vol, s0, t_end, x.max(), phase=True, refill_lanes=rl)
+        for k in ("rf", "sf", "phase", "nsteps", "status"):
+            assert torch.equal(o[k], ref[k]), (rl, k)
+    E1 = _small_ensemble(tune=False, mode="one_launch")
+    torch.cuda.synchronize()
+    out1 = {k: v.clone() for k, v in E1.out.items()}
+    E1.refill = 32
+    E1._trace_only()
+    torch.cuda.synchronize()
+    for k in ("rf", "phase", "nsteps", "status"):
+        assert torch.equal(E1.out[k], out1[k]), k
+
+
 def test_graph_replay_matches_eager(cuda):
     E = _small_ensemble(tune=False)
     torch.cuda.synchronize()

@@ -55,7 +55,7 @@ class TTVolume(ctypes.Structure):
 class TTTraceOpts(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double), ("atol_phase", ctypes.c_double),
                 ("max_steps", ctypes.c_int64), ("with_phase", ctypes.c_int32), ("block_size", ctypes.c_int32),
-                ("ray_chunk", ctypes.c_int32), ("phase_f64", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("ray_chunk", ctypes.c_int32), ("phase_f64", ctypes.c_int32), ("refill_lanes", ctypes.c_int32)]
 
 
 TT_RK_MAX_STAGES = 16

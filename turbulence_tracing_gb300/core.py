@@ -213,9 +213,11 @@ def rebuild_volume(vol):
 # ---------------------------------------------------------------------------
 # K2
 # ---------------------------------------------------------------------------
-def _opts(rtol, atol, atol_phase, max_steps, with_phase, block_size=0, ray_chunk=0, phase_f64=False):
+def _opts(rtol, atol, atol_phase, max_steps, with_phase, block_size=0, ray_chunk=0, phase_f64=False,
+          refill_lanes=0):
     o = _lib.TTTraceOpts()
     o.phase_f64 = 1 if phase_f64 else 0
+    o.refill_lanes = int(refill_lanes or 0)
     o.rtol = float(rtol)
     o.atol = float(atol)
     o.atol_phase = float(atol_phase)
@@ -304,9 +306,11 @@ def trace_f64(fields, s0, t_end, probing_axis, extent, rtol=1e-3, atol=1e-6, pha
 
 
 def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, phase=False, max_steps=None,
-              want_sf=True, ws=None, out=None, block_size=0, ray_chunk=0, phase_f64=False):
+              want_sf=True, ws=None, out=None, block_size=0, ray_chunk=0, phase_f64=False, refill_lanes=0):
     """Persistent FP32 tracer over a Volume32.  s0: (6, Np) float64.
-    phase_f64: accumulate the phase in FP64 rather than a compensated FP32 pair."""
+    phase_f64: accumulate the phase in FP64 rather than a compensated FP32 pair.
+    refill_lanes: a warp takes new rays once this many lanes are idle (0 = 1;
+    32 keeps a warp on 32 neighbouring rays to the end; results are the same)."""
     dev = require_cuda()
     L = _lib.lib()
     s0_t = _f64_dev(s0, dev)
@@ -318,7 +322,7 @@ def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, pha
     need = L.tt_trace_f32_workspace_bytes(ctypes.byref(vol.desc), np_)
     if ws is None or ws.numel() < need:
         ws = workspace(need, dev)
-    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size, ray_chunk, phase_f64)
+    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size, ray_chunk, phase_f64, refill_lanes)
     check(L.tt_trace_f32(ctypes.byref(vol.desc), _ptr(s0_t), np_, float(t_end), float(extent), ctypes.byref(o),
                          _ptr(out["sf"]), _ptr(out["rf"]), _ptr(out["phase"]) if phase else None,
                          _ptr(out["status"]), _ptr(out["nsteps"]), _ptr(ws), ws.numel(), _stream()),
@@ -328,7 +332,8 @@ def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, pha
 
 
 def trace_f32_batched(vols, s0, ray_offsets, t_ends, extents, rtol=1e-7, atol=1e-5, atol_phase=1e-5,
-                      phase=False, max_steps=None, want_sf=True, ws=None, out=None, block_size=0, ray_chunk=0):
+                      phase=False, max_steps=None, want_sf=True, ws=None, out=None, block_size=0, ray_chunk=0,
+                      refill_lanes=0):
     """All instances in one persistent launch.  s0 is the instance-blocked ray
     array: a flat float64 tensor holding instance i's (6, n_i) block at
     6 * ray_offsets[i].  Outputs are blocked the same way (see ray_block)."""
@@ -355,7 +360,7 @@ def trace_f32_batched(vols, s0, ray_offsets, t_ends, extents, rtol=1e-7, atol=1e
     need = L.tt_trace_f32_batched_workspace_bytes(descs, n, ntot)
     if ws is None or ws.numel() < need:
         ws = workspace(need, dev)
-    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size, ray_chunk)
+    o = _opts(rtol, atol, atol_phase, max_steps, phase, block_size, ray_chunk, refill_lanes=refill_lanes)
     dp = ctypes.POINTER(ctypes.c_double)
     check(L.tt_trace_f32_batched(descs, n, offs.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), te.ctypes.data_as(dp),
                                  ex.ctypes.data_as(dp), _ptr(s0_t), ctypes.byref(o), _ptr(out["sf"]), _ptr(out["rf"]),

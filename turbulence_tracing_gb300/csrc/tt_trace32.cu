@@ -145,6 +145,7 @@ struct Ctl {
     int with_phase;
     int phase_f64;  // accumulate the phase in FP64 (else a Neumaier-compensated FP32 pair)
     int chunk;  // rays a warp takes from the work counter at a time (>= 32)
+    int refill;  // a warp takes new rays once at least this many lanes are idle (1..32)
     long long max_steps;
 };
 
@@ -843,7 +844,9 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
     for (;;) {
         const bool need = !busy && !drained;
         const unsigned mask = __ballot_sync(0xffffffffu, need);
-        if (mask) {
+        // refill once K.refill lanes are idle (or none is busy): with 32, a
+        // warp's lanes trace 32 neighbouring rays together to the end
+        if (mask && (K.refill <= 1 || __popc(mask) >= K.refill || __ballot_sync(0xffffffffu, busy) == 0u)) {
             // lanes are refilled from the warp's chunk of consecutive bucketed
             // rays; a new chunk comes from the shared work counter.  (Larger
             // chunks, and per-block segments with stealing, both measured slower.)
@@ -1114,6 +1117,9 @@ int make_ctl(const tt_trace_opts* opts, Ctl* K)
     const int ch = opts->ray_chunk;
     if (ch != 0 && (ch < 32 || ch > 1024 || ch % 32)) return tt::invalid("trace_f32: ray_chunk must be 0 or 32..1024, a multiple of 32");
     K->chunk = ch ? ch : 32;  // 32 measured fastest
+    const int rl = opts->refill_lanes;
+    if (rl < 0 || rl > 32) return tt::invalid("trace_f32: refill_lanes must be 0..32");
+    K->refill = rl ? rl : 1;
     return TT_OK;
 }
 

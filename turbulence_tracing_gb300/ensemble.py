@@ -33,6 +33,7 @@ import torch
 from . import _lib, autotune, core, turboGen
 
 C_LIGHT = 299792458.0
+REFILLS = (1, 32)  # lane refill thresholds the set-up times (tt_trace_opts.refill_lanes)
 
 
 def draw_instances(n_inst=64, seed=0, sizes=(128, 192, 256, 384), exponents=(-5.0 / 3.0, -3.0, -11.0 / 3.0),
@@ -65,13 +66,14 @@ def gaussian_beam_into(dst, nrays, sigma, divergence, extent, rng):
 
 class Ensemble:
     def __init__(self, instances, L=2e-3, sigma_frac=0.25, divergence=0.05e-3, lwl=1064e-9, det=512,
-                 phase=False, rtol=1e-7, tune=True, tune_rays=200000, beam_seed=1, mode="grouped"):
+                 phase=False, rtol=1e-7, tune=True, tune_rays=200000, beam_seed=1, mode="grouped", refill_lanes=1):
         order = sorted(range(len(instances)), key=lambda i: instances[i]["n"])
         self.order = order  # instance k here is instances[order[k]]
         self.inst = [instances[i] for i in order]
         if mode not in ("grouped", "one_launch", "per_instance"):
             raise ValueError("mode must be grouped, one_launch or per_instance")
         self.mode = mode
+        self.refill = int(refill_lanes)
         self.L, self.sigma, self.div, self.lwl, self.det = L, sigma_frac * L, divergence, lwl, det
         self.phase, self.rtol = phase, rtol
         self.tune, self.tune_rays, self.beam_seed = tune, tune_rays, beam_seed
@@ -139,12 +141,15 @@ class Ensemble:
         self.step()  # allocates outputs and workspace once
         torch.cuda.synchronize()
         if self.tune:
-            # launch mode, then the block size of the chosen mode, timed on the ensemble itself
+            # launch mode and lane refill (every idle lane at once, or a warp's
+            # 32 lanes together), then the block size, timed on the ensemble itself
             self.mode_ms = {}
-            for m in ("grouped", "per_instance"):
-                self.mode = m
-                self.mode_ms[m] = autotune._time(self._trace_only, 1)
-            self.mode = min(self.mode_ms, key=self.mode_ms.get)
+            for m in ("grouped", "per_instance", "one_launch"):
+                for rl in REFILLS:
+                    self.mode, self.refill = m, rl
+                    self.mode_ms["%s/%d" % (m, rl)] = autotune._time(self._trace_only, 1)
+            best = min(self.mode_ms, key=self.mode_ms.get)
+            self.mode, self.refill = best.split("/")[0], int(best.split("/")[1])
             self.block_ms = {}
             for b in autotune.BLOCKS:
                 self.block = b
@@ -178,7 +183,8 @@ class Ensemble:
                     for k, v in self.out.items() if not k.startswith("_")}
             o = core.trace_f32_batched(self.vols[a:b], self.s0[6 * r0:6 * r1], self.offsets[a:b + 1] - r0,
                                        self.t_ends[a:b], self.extents[a:b], rtol=self.rtol, phase=self.phase,
-                                       out=view, ws=self.ws.get((self.mode, a)), block_size=self.block)
+                                       out=view, ws=self.ws.get((self.mode, a)), block_size=self.block,
+                                       refill_lanes=self.refill)
             self.ws[(self.mode, a)] = o["_ws"]
 
     # ------------------------------------------------------------------ one pass
@@ -211,8 +217,9 @@ class Ensemble:
 
     # ------------------------------------------------------------------ reference form
     def run_unbatched(self):
-        """The same work one instance at a time (one trace launch per instance),
-        without a graph: the comparison point for batching."""
+        """The same work one instance at a time (one trace launch per instance,
+        the tracer's default options), without a graph: the comparison point
+        for batching."""
         outs = []
         for i, v in enumerate(self.vols):
             core.rebuild_volume(v)
@@ -249,8 +256,9 @@ def _main(argv=None):
     E = Ensemble(inst, tune=False).setup()
     res = {}
     for m in ("grouped", "one_launch", "per_instance"):
-        E.mode = m
-        res[m] = autotune._time(E._trace_only, a.reps)
+        for rl in REFILLS:
+            E.mode, E.refill = m, rl
+            res["%s/%d" % (m, rl)] = autotune._time(E._trace_only, a.reps)
     print(json.dumps({"instances": len(inst), "rays": E.ntot, "trace_ms_by_mode": res}))
 
 

@@ -275,6 +275,7 @@ struct Ray {
     float fr[3];
     float u[3];
     float sig, sigc;
+    float uc[3];     // compensation of u (Kahan)
     float ph, phc;   // phase: Neumaier pair, or (FP64 accumulation) the two words of one double
     float hctrl;
     float hcap;    // one-shot cap on the next attempt after a face-crossing rejection
@@ -428,6 +429,7 @@ __device__ __forceinline__ bool init_ray(const Geo& G, const Src& src, const dou
     R.natt = R.nacc = 0;
     R.sig = R.sigc = 0.f;
     R.ph = R.phc = 0.f;
+    R.uc[0] = R.uc[1] = R.uc[2] = 0.f;
     R.hctrl = 1.0f;
     R.hcap = 3.0e38f;
     R.rejected = false;
@@ -503,7 +505,7 @@ __device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const R
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             P[a] = (double)R.ci[a] + (double)R.fr[a];
-            u[a] = (double)R.u[a];
+            u[a] = (double)R.u[a] - (double)R.uc[a];
         }
         if (R.state == 1 && R.code == TT_RAY_OK) ds = G.sig_end - sig > 0.0 ? G.sig_end - sig : 0.0;
     } else {
@@ -617,15 +619,25 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     for (int a = 0; a < 3; ++a) {
         const float vel = G.r[a] * R.u[a];
         const float acc = G.r[a] * Hs[0][a];
-        const float hu = first_hit(vel, acc, 1.f - R.fr[a]);
-        const float hl = first_hit(-vel, -acc, R.fr[a]);
+        // the face ahead is reached first if the ray gets there before it
+        // turns back; otherwise the face behind (the same root as the
+        // smaller of the two face times)
+        const bool up = vel >= 0.f;
+        float v1 = up ? vel : -vel, a1 = up ? acc : -acc;
+        float d1 = up ? 1.f - R.fr[a] : R.fr[a];
+        if (!(d1 > 0.f) || fmaf(v1, v1, 2.f * a1 * d1) < 0.f) {
+            v1 = -v1;
+            a1 = -a1;
+            d1 = up ? R.fr[a] : 1.f - R.fr[a];
+        }
+        const float hfa = first_hit(v1, a1, d1);
         const bool box_up = R.ci[a] == G.n[a] - 2, box_lo = R.ci[a] == 0;
         if ((box_up && vel > 0.f && (1.f - R.fr[a]) <= kBoxPath * vel) ||
             (box_lo && vel < 0.f && R.fr[a] <= -kBoxPath * vel)) {
             R.state = 1;
             return;
         }
-        hf = fminf(hf, fminf(hu, hl));
+        hf = fminf(hf, hfa);
     }
     ++R.natt;
     bool last = false;
@@ -636,7 +648,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         last = true;
     }
     float phb = 0.f, phe = 0.f;
-    float Pn[3], un[3];
+    float Pn[3], un[3], inc6[3];
     if (K.with_phase) {
         const float u2 = fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2]));
         const float sp = sqrt_apx(u2);
@@ -663,6 +675,10 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
             const float2 pp = __ffma2_rn(hr2, __ffma2_rn(make_float2(fc(s), fc(s)), u2v, __fmul2_rn(h2, saa)), fr2);
             us[0] = uu.x;
             us[1] = uu.y;
+            if (s == 6) {
+                inc6[0] = sa.x;
+                inc6[1] = sa.y;
+            }
             Ps[0] = pp.x;
             Ps[1] = pp.y;
         }
@@ -675,6 +691,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
                 if (k + 1 < s && !(s == 6 && k == 1)) saa = fmaf(faa(s, k), Hs[k][c], saa);
             }
             us[c] = fmaf(h, sa, R.u[c]);
+            if (s == 6) inc6[c] = sa;
             Ps[c] = fmaf(h * G.r[c], fmaf(fc(s), R.u[c], h * saa), R.fr[c]);
         }
         float q;
@@ -721,12 +738,11 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         eus[2] = eu; eps[2] = ep;
     }
     float es = 0.f;
+    const float hs = h * inv_scu, hp = h * h * K.inv_atol_cells;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float eu = eus[c] * h;
-        const float ep = eps[c] * (h * h * G.r[c]);
-        const float x1 = eu * inv_scu;
-        const float x2 = ep * K.inv_atol_cells;
+        const float x1 = eus[c] * hs;
+        const float x2 = eps[c] * (hp * G.r[c]);
         es = fmaf(x1, x1, fmaf(x2, x2, es));
     }
     int neq = 6;
@@ -740,14 +756,15 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         es = fmaf(x, x, es);
         neq = 7;
     }
-    const float en = sqrtf(es * (neq == 7 ? (1.f / 7.f) : (1.f / 6.f)));
-    if (!(en == en)) {
+    // the squared RMS error norm: the controller's en^-1/5 is (en^2)^-1/10
+    const float en2 = es * (neq == 7 ? (1.f / 7.f) : (1.f / 6.f));
+    if (!(en2 == en2)) {
         R.code = TT_RAY_NAN;
         R.state = 3;
         return;
     }
-    if (en >= 1.0f) {
-        const float factor = fmaxf(0.2f, 0.9f * __powf(en, -0.2f));
+    if (en2 >= 1.0f) {
+        const float factor = fmaxf(0.2f, 0.9f * __powf(en2, -0.1f));
         R.hctrl = h * factor;
         R.rejected = true;
         if (R.hctrl < 1e-7f) {
@@ -781,7 +798,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         R.hcap = hre;  // controller state untouched: this was a geometric retry
         return;
     }
-    float factor = en == 0.f ? 10.f : fminf(10.f, 0.9f * __powf(en, -0.2f));
+    float factor = en2 == 0.f ? 10.f : fminf(10.f, 0.9f * __powf(en2, -0.1f));
     if (R.rejected) factor = fminf(1.f, factor);
     R.rejected = false;
     R.hctrl = h * factor;
@@ -789,7 +806,13 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         R.fr[c] = Pn[c];
-        R.u[c] = un[c];
+        // u is a compensated sum of the accepted increments h (b . H): FP32
+        // rounding of u itself, ~6e-8 per step, would otherwise random-walk
+        // to ~1e-6 rad over a few hundred strongly deflecting steps
+        const float y = fmaf(h, inc6[c], -R.uc[c]);
+        const float t = __fadd_rn(R.u[c], y);
+        R.uc[c] = __fsub_rn(__fsub_rn(t, R.u[c]), y);
+        R.u[c] = t;
     }
     {  // Kahan on sigma
         const float y = __fsub_rn(h, R.sigc);

@@ -422,10 +422,11 @@ class Pipeline:
 
 class BatchedTracer:
     """The exact method at its best throughput: a chunk of fields traced in one
-    batched persistent launch (tt_trace_f32_batched), then their shadowgrams."""
+    batched persistent launch (tt_trace_f32_batched), then their shadowgrams.
+    refill_lanes as tt_trace_opts (results do not depend on it)."""
 
-    def __init__(self, W, batch=8):
-        self.W, self.B = W, batch
+    def __init__(self, W, batch=8, refill_lanes=0):
+        self.W, self.B, self.refill = W, batch, refill_lanes
         self.vols = [None] * batch
         self.s0 = W.s0.reshape(-1).repeat(batch)
         self.out = None
@@ -444,7 +445,7 @@ class BatchedTracer:
             if self.out is not None and n != self.B:
                 self.out = None
             o = core.trace_f32_batched(self.vols[:n], self.s0[:6 * S * S * n], offs, [W.t_end] * n, [W.ext] * n,
-                                       rtol=W.rtol, phase=True, want_sf=False,
+                                       rtol=W.rtol, phase=True, want_sf=False, refill_lanes=self.refill,
                                        ws=None if self.out is None else self.out["_ws"], out=self.out)
             self.out = o if n == self.B else None
             for i in range(n):

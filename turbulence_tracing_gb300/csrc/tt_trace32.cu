@@ -550,6 +550,7 @@ __device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const R
 // Right-hand side at stage position Ps (fractions in the current cell):
 // the current cell's polynomial while Ps stays within kTolE of it (never past
 // a box face), the exact lookup otherwise.
+template <bool PHASE>
 __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, const Ray& R,
                                            const float2 (*coef)[8], const float Ps[3], float H[3], float& q)
 {
@@ -566,7 +567,7 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restric
         H[0] = hab.x;
         H[1] = hab.y;
         H[2] = hcq.x;
-        q = K.with_phase ? hcq.y : 0.f;
+        q = PHASE ? hcq.y : 0.f;
     } else {
         const float4 r = eval_exact(nodes, G.n[0], G.n[1], G.n[2], G.st_b, G.tile_f4, G.bd, G.bd_shift,
                                     G.brick_f4, R.ci[0], R.ci[1], R.ci[2], Ps[0], Ps[1], Ps[2]);
@@ -577,7 +578,11 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restric
     }
 }
 
-// One attempted step.  Returns with R updated.
+// One attempted step.  Returns with R updated.  PHASE (the phase integrated as
+// a seventh equation) is a template parameter: a run-time flag put a branch
+// in every stage, which split the unrolled stage loop into blocks the
+// compiler schedules separately (5.7% slower with the phase on).
+template <bool PHASE>
 __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, Ray& R,
                                      float2 (*coef)[8])
 {
@@ -609,7 +614,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         Hs[0][0] = hab.x;
         Hs[0][1] = hab.y;
         Hs[0][2] = hcq.x;
-        q0 = K.with_phase ? hcq.y : 0.f;
+        q0 = PHASE ? hcq.y : 0.f;
     }
     // Predict the first face crossing of the cell from position, velocity and
     // acceleration; aim the step end at it.  Leaving through a box face within
@@ -649,7 +654,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     }
     float phb = 0.f, phe = 0.f;
     float Pn[3], un[3], inc6[3];
-    if (K.with_phase) {
+    if (PHASE) {
         const float u2 = fmaf(R.u[0], R.u[0], fmaf(R.u[1], R.u[1], R.u[2] * R.u[2]));
         const float sp = sqrt_apx(u2);
         const float dph = G.kappa * nm1f(q0) * sp;
@@ -695,10 +700,10 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
             Ps[c] = fmaf(h * G.r[c], fmaf(fc(s), R.u[c], h * saa), R.fr[c]);
         }
         float q;
-        stage_eval(G, nodes, K, R, coef, Ps, Hs[s], q);
+        stage_eval<PHASE>(G, nodes, K, R, coef, Ps, Hs[s], q);
         // Dormand-Prince's b and e weights of stage 1 are zero: its phase rate
         // is not needed (the sums are unchanged: an FMA with weight 0 adds an exact 0)
-        if (K.with_phase && s != 1) {
+        if (PHASE && s != 1) {
             const float u2 = fmaf(us[0], us[0], fmaf(us[1], us[1], us[2] * us[2]));
             const float sp = sqrt_apx(u2);
             const float dph = G.kappa * nm1f(q) * sp;
@@ -747,7 +752,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     }
     int neq = 6;
     float dphi = 0.f;
-    if (K.with_phase) {
+    if (PHASE) {
         dphi = h * phb;
         const float phv = K.phase_f64 ? (float)ph_get(R) : R.ph;
         const float phn = phv + dphi;
@@ -820,7 +825,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         R.sigc = __fsub_rn(__fsub_rn(t, R.sig), y);
         R.sig = t;
     }
-    if (K.with_phase) {
+    if (PHASE) {
         if (K.phase_f64) ph_set(R, ph_get(R) + (double)dphi);
         else neumaier(R.ph, R.phc, dphi);
     }
@@ -846,7 +851,7 @@ __device__ __forceinline__ int instance_of(const Geo* g, int n, long long r)
 // block (src: node buffer and the block of the instance-blocked arrays).  It
 // is asked once per fetched ray; the node pointer is kept for the ray's steps
 // unless the policy has it as a constant (pol.nodes).
-template <typename Policy>
+template <bool PHASE, typename Policy>
 __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const double* __restrict__ s0,
                                                 long long np, const unsigned* __restrict__ perm,
                                                 unsigned long long* __restrict__ counter, double* __restrict__ sf,
@@ -922,7 +927,7 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
         }
         if (__ballot_sync(0xffffffffu, busy || (!drained)) == 0u) break;
         if (busy) {
-            step(pol.geo(ray), pol.nodes(nodes), K, R, coef);
+            step<PHASE>(pol.geo(ray), pol.nodes(nodes), K, R, coef);
             if (R.state != 0) {
                 finish_ray<true>(pol.geo(ray), pol.src(ray), R, nullptr, nullptr, ray, np, sf, rf, phase, status,
                                  nsteps, K.phase_f64 != 0);
@@ -939,14 +944,14 @@ struct SinglePolicy {
     __device__ __forceinline__ const float4* nodes(const float4*) const { return g->nodes; }
 };
 
-template <int BLOCK>
+template <int BLOCK, bool PHASE>
 __global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
 trace32_kernel(const Geo G, Ctl K, const double* __restrict__ s0, long long np,
                const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
                double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
                int* __restrict__ status, int* __restrict__ nsteps)
 {
-    persistent_loop(SinglePolicy{&G}, K, s0, np, perm, counter, sf, rf, phase, status, nsteps);
+    persistent_loop<PHASE>(SinglePolicy{&G}, K, s0, np, perm, counter, sf, rf, phase, status, nsteps);
 }
 
 // Volumes of different shapes: each lane reads its ray's instance entry from
@@ -976,15 +981,15 @@ struct MixedPolicy {
     __device__ __forceinline__ const float4* nodes(const float4* kept) const { return kept; }
 };
 
-template <int BLOCK>
+template <int BLOCK, bool PHASE>
 __global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
 trace32_batched_kernel(const __grid_constant__ GeoTable table, Ctl K, const double* __restrict__ s0, long long np,
                        const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
                        double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
                        int* __restrict__ status, int* __restrict__ nsteps)
 {
-    persistent_loop(MixedPolicy{table.g, table.n, -1, table.g}, K, s0, np, perm, counter, sf, rf, phase, status,
-                    nsteps);
+    persistent_loop<PHASE>(MixedPolicy{table.g, table.n, -1, table.g}, K, s0, np, perm, counter, sf, rf, phase,
+                           status, nsteps);
 }
 
 // Volumes of one shape (grid, spacing, brick depth, t_end): the geometry is
@@ -1004,14 +1009,14 @@ struct UniformPolicy {
     __device__ __forceinline__ const float4* nodes(const float4* kept) const { return kept; }
 };
 
-template <int BLOCK>
+template <int BLOCK, bool PHASE>
 __global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
 trace32_uniform_kernel(const __grid_constant__ GeoTable table, Ctl K, const double* __restrict__ s0,
                        long long np, const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
                        double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
                        int* __restrict__ status, int* __restrict__ nsteps)
 {
-    persistent_loop(UniformPolicy{table.g, table.n}, K, s0, np, perm, counter, sf, rf, phase, status, nsteps);
+    persistent_loop<PHASE>(UniformPolicy{table.g, table.n}, K, s0, np, perm, counter, sf, rf, phase, status, nsteps);
 }
 
 // --- ray bucketing by (instance, entry tile) ----------------------------------
@@ -1138,7 +1143,8 @@ int make_ctl(const tt_trace_opts* opts, Ctl* K)
     K->phase_f64 = (opts->with_phase && opts->phase_f64) ? 1 : 0;
     K->max_steps = opts->max_steps > 0 ? opts->max_steps : TT_DEFAULT_MAX_STEPS;
     const int ch = opts->ray_chunk;
-    if (ch != 0 && (ch < 32 || ch > 1024 || ch % 32)) return tt::invalid("trace_f32: ray_chunk must be 0 or 32..1024, a multiple of 32");
+    if (ch != 0 && (ch < 32 || ch > 1024 || ch % 32))
+        return tt::invalid("trace_f32: ray_chunk must be 0 or 32..1024, a multiple of 32");
     K->chunk = ch ? ch : 32;  // 32 measured fastest
     const int rl = opts->refill_lanes;
     if (rl < 0 || rl > 32) return tt::invalid("trace_f32: refill_lanes must be 0..32");
@@ -1168,7 +1174,7 @@ template <typename KernelT>
 int occupancy_grid(KernelT kernel, int block, int slot)
 {
     // per-(kernel, device) cache; threads may race to fill an entry, all with the same value
-    static std::atomic<int> cache[9][64];
+    static std::atomic<int> cache[18][64];
     int dev = 0;
     cudaGetDevice(&dev);
     int b = (dev >= 0 && dev < 64) ? cache[slot][dev].load(std::memory_order_relaxed) : 0;
@@ -1228,15 +1234,21 @@ int run(const GeoTable& table, int nbins, const Ctl& K, int block, const double*
     bin_scatter_kernel<<<bin_grid(np), 256, 0, s>>>(table, s0, np, cnt, perm);
     TT_TRY(tt::launch_status("trace_f32 ray binning"));
     const Ctl& Kc = K;
-#define TT_LAUNCH_SINGLE(BS, SLOT)                                                                    \
-    trace32_kernel<BS><<<occupancy_grid(trace32_kernel<BS>, BS, SLOT), BS, 0, s>>>(                  \
-        table.g[0], Kc, s0, np, perm, counter, sf, rf, phase, status, nsteps)
-#define TT_LAUNCH_BATCH(BS, SLOT)                                                                     \
-    trace32_batched_kernel<BS><<<occupancy_grid(trace32_batched_kernel<BS>, BS, SLOT), BS, 0, s>>>(  \
-        table, Kc, s0, np, perm, counter, sf, rf, phase, status, nsteps)
-#define TT_LAUNCH_UNIFORM(BS, SLOT)                                                                   \
-    trace32_uniform_kernel<BS><<<occupancy_grid(trace32_uniform_kernel<BS>, BS, SLOT), BS, 0, s>>>(  \
-        table, Kc, s0, np, perm, counter, sf, rf, phase, status, nsteps)
+#define TT_LAUNCH_ONE(KERNEL, ARGS, BS, SLOT)                                                         \
+    do {                                                                                              \
+        if (Kc.with_phase)                                                                            \
+            KERNEL<BS, true><<<occupancy_grid(KERNEL<BS, true>, BS, (SLOT) + 9), BS, 0, s>>> ARGS;    \
+        else                                                                                          \
+            KERNEL<BS, false><<<occupancy_grid(KERNEL<BS, false>, BS, SLOT), BS, 0, s>>> ARGS;        \
+    } while (0)
+#define TT_LAUNCH_SINGLE(BS, SLOT) \
+    TT_LAUNCH_ONE(trace32_kernel, (table.g[0], Kc, s0, np, perm, counter, sf, rf, phase, status, nsteps), BS, SLOT)
+#define TT_LAUNCH_BATCH(BS, SLOT)                                                                         \
+    TT_LAUNCH_ONE(trace32_batched_kernel, (table, Kc, s0, np, perm, counter, sf, rf, phase, status, nsteps), BS, \
+                  SLOT)
+#define TT_LAUNCH_UNIFORM(BS, SLOT)                                                                       \
+    TT_LAUNCH_ONE(trace32_uniform_kernel, (table, Kc, s0, np, perm, counter, sf, rf, phase, status, nsteps), BS, \
+                  SLOT)
     // block 0 = 256 (measured fastest on the 256^3 and 512^3 workloads)
     if (table.n == 1) {
         if (block == 64) TT_LAUNCH_SINGLE(64, 0);
@@ -1254,6 +1266,7 @@ int run(const GeoTable& table, int nbins, const Ctl& K, int block, const double*
 #undef TT_LAUNCH_SINGLE
 #undef TT_LAUNCH_BATCH
 #undef TT_LAUNCH_UNIFORM
+#undef TT_LAUNCH_ONE
     return tt::launch_status("trace_f32 kernel");
 }
 

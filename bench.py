@@ -42,8 +42,8 @@ ALG_BYTES_PHASE = 768  # 6 stages x 8 corners x 4 components x 4 B per ray-step 
 # profiles/trace32_grf512_1e7rays_counters.md): warp instructions issued and
 # DRAM bytes.  The bench line scales them by accepted ray-steps for other
 # workloads and says so.
-TRACE32_CAPTURE = {"workload": "grf512_1e+07rays_phase_3det1024", "ray_steps": 4225486610,
-                   "warp_inst": 194081634571, "dram_read_bytes": 20.48e9, "dram_write_bytes": 5.84e9}
+TRACE32_CAPTURE = {"workload": "grf512_1e+07rays_phase_3det1024", "ray_steps": 4225457556,
+                   "warp_inst": 156168768481, "dram_read_bytes": 20604839168, "dram_write_bytes": 5846129920}
 
 
 def parse():

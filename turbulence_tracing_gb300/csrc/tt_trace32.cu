@@ -552,15 +552,12 @@ __device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const R
 // a box face), the exact lookup otherwise.
 template <bool PHASE>
 __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, const Ray& R,
-                                           const float2 (*coef)[8], const float Ps[3], float H[3], float& q)
+                                           const float2 (*coef)[8], const float Ps[3], float H[3], float& q,
+                                           const float* lo, const float* hi)
 {
     bool home = true;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float lo = R.ci[a] == 0 ? 0.f : -kTolE;
-        const float hi = R.ci[a] == G.n[a] - 2 ? 1.f : 1.f + kTolE;
-        home = home && Ps[a] >= lo && Ps[a] <= hi;
-    }
+    for (int a = 0; a < 3; ++a) home = home && Ps[a] >= lo[a] && Ps[a] <= hi[a];
     if (home) {
         const float2 hab = tri2(coef[0], Ps[0], Ps[1], Ps[2]);
         const float2 hcq = tri2(coef[1], Ps[0], Ps[1], Ps[2]);
@@ -661,6 +658,15 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         phb = fa(6, 0) * dph;
         phe = fe(0) * dph;
     }
+    // The cell's in-cell bounds for the stage tests (no tolerance at a box
+    // face), formed once per step: left to stage_eval, the compare-and-select
+    // was rebuilt in every stage (5% of the step's time).
+    float blo[3], bhi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        blo[a] = R.ci[a] == 0 ? 0.f : -kTolE;
+        bhi[a] = R.ci[a] == G.n[a] - 2 ? 1.f : 1.f + kTolE;
+    }
     const float2 h2 = make_float2(h, h);
     const float2 hr2 = make_float2(h * G.r[0], h * G.r[1]);
     const float2 u2v = make_float2(R.u[0], R.u[1]);
@@ -700,7 +706,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
             Ps[c] = fmaf(h * G.r[c], fmaf(fc(s), R.u[c], h * saa), R.fr[c]);
         }
         float q;
-        stage_eval<PHASE>(G, nodes, K, R, coef, Ps, Hs[s], q);
+        stage_eval<PHASE>(G, nodes, K, R, coef, Ps, Hs[s], q, blo, bhi);
         // Dormand-Prince's b and e weights of stage 1 are zero: its phase rate
         // is not needed (the sums are unchanged: an FMA with weight 0 adds an exact 0)
         if (PHASE && s != 1) {

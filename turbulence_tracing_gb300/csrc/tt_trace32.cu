@@ -930,8 +930,11 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
             } else {
                 wnext += cnt;
             }
+            // only a refill can leave the warp with nothing to do: every lane
+            // is then busy or drained (a lane whose ray missed the box is
+            // neither, and takes another on the next pass)
+            if (__ballot_sync(0xffffffffu, busy || (!drained)) == 0u) break;
         }
-        if (__ballot_sync(0xffffffffu, busy || (!drained)) == 0u) break;
         if (busy) {
             step<PHASE>(pol.geo(ray), pol.nodes(nodes), K, R, coef);
             if (R.state != 0) {

@@ -509,7 +509,8 @@ def surrogate_run(a):
     workload at that grid: data made by the tracer itself, FNO training by the
     library's kernels, held-out evaluation against the exact tracer, then the
     surrogate-with-fallback pipeline timed against tracing every field (one
-    field per launch, and a chunk of fields per batched launch)."""
+    field per launch, and a chunk of fields per batched launch with either
+    lane-refill rule, the faster of the two being the baseline)."""
     import time
 
     import torch

@@ -617,6 +617,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     // acceleration; aim the step end at it.  Leaving through a box face within
     // kBoxPath: the ray has left (the field beyond is the fill value 0).
     float hf = 3.0e38f;
+    bool leave = false;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float vel = G.r[a] * R.u[a];
@@ -634,12 +635,13 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         }
         const float hfa = first_hit(v1, a1, d1);
         const bool box_up = R.ci[a] == G.n[a] - 2, box_lo = R.ci[a] == 0;
-        if ((box_up && vel > 0.f && (1.f - R.fr[a]) <= kBoxPath * vel) ||
-            (box_lo && vel < 0.f && R.fr[a] <= -kBoxPath * vel)) {
-            R.state = 1;
-            return;
-        }
+        leave = leave || (box_up && vel > 0.f && (1.f - R.fr[a]) <= kBoxPath * vel) ||
+                (box_lo && vel < 0.f && R.fr[a] <= -kBoxPath * vel);
         hf = fminf(hf, hfa);
+    }
+    if (leave) {  // within kBoxPath of a box face it is moving through: it has left
+        R.state = 1;
+        return;
     }
     ++R.natt;
     bool last = false;
@@ -790,20 +792,16 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float vend = G.r[a] * un[a];
-        float over = 0.f;  // path past the crossed face
-        bool box = false;
-        if (Pn[a] > 1.f && R.fr[a] <= 1.f) {
-            over = __fdividef(Pn[a] - 1.f, fmaxf(vend, 1e-6f));
-            box = R.ci[a] == G.n[a] - 2;
-        } else if (Pn[a] < 0.f && R.fr[a] >= 0.f) {
-            over = __fdividef(-Pn[a], fmaxf(-vend, 1e-6f));
-            box = R.ci[a] == 0;
-        }
-        if (over > (box ? kBoxPath : kFacePath)) {
-            float hn = h - 1.01f * over;
-            if (!(hn > 0.1f * h)) hn = 0.5f * h;
-            hre = fminf(hre, hn);
-        }
+        // path past the crossed face, without branches
+        const bool xu = Pn[a] > 1.f && R.fr[a] <= 1.f;
+        const bool xl = !xu && Pn[a] < 0.f && R.fr[a] >= 0.f;
+        const float num = xu ? Pn[a] - 1.f : -Pn[a];
+        const float den = fmaxf(xu ? vend : -vend, 1e-6f);
+        const float over = (xu || xl) ? __fdividef(num, den) : 0.f;
+        const bool box = xu ? R.ci[a] == G.n[a] - 2 : (xl && R.ci[a] == 0);
+        float hn = h - 1.01f * over;
+        if (!(hn > 0.1f * h)) hn = 0.5f * h;
+        hre = over > (box ? kBoxPath : kFacePath) ? fminf(hre, hn) : hre;
     }
     if (hre < 3.0e38f) {
         R.hcap = hre;  // controller state untouched: this was a geometric retry

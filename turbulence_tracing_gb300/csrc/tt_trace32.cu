@@ -594,13 +594,9 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         R.cell_dirty = false;
     }
     const float rem = (G.sig_end_f - R.sig) - R.sigc;
-    if (!(rem > 0.f)) {
-        R.state = 2;
-        return;
-    }
-    if (R.natt >= K.max_steps) {
-        R.code = TT_RAY_MAX_STEPS;
-        R.state = 3;
+    if (!(rem > 0.f) || R.natt >= K.max_steps) {  // at t_end, or out of attempts
+        if (rem > 0.f) R.code = TT_RAY_MAX_STEPS;
+        R.state = rem > 0.f ? 3 : 2;
         return;
     }
     float Hs[7][3];
@@ -771,21 +767,6 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     }
     // the squared RMS error norm: the controller's en^-1/5 is (en^2)^-1/10
     const float en2 = es * (neq == 7 ? (1.f / 7.f) : (1.f / 6.f));
-    if (!(en2 == en2)) {
-        R.code = TT_RAY_NAN;
-        R.state = 3;
-        return;
-    }
-    if (en2 >= 1.0f) {
-        const float factor = fmaxf(0.2f, 0.9f * __powf(en2, -0.1f));
-        R.hctrl = h * factor;
-        R.rejected = true;
-        if (R.hctrl < 1e-7f) {
-            R.code = TT_RAY_STEP_TOO_SMALL;
-            R.state = 3;
-        }
-        return;
-    }
     // Where did the step cross a face?  If it ran too far past one, redo it
     // ending at the crossing (estimated backwards from the end point).
     float hre = 3.0e38f;
@@ -803,8 +784,23 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         if (!(hn > 0.1f * h)) hn = 0.5f * h;
         hre = over > (box ? kBoxPath : kFacePath) ? fminf(hre, hn) : hre;
     }
-    if (hre < 3.0e38f) {
-        R.hcap = hre;  // controller state untouched: this was a geometric retry
+    // one branch off the accepted path: a NaN, then a rejected error, then a
+    // face-crossing retry, in that order
+    if (!(en2 < 1.0f) || hre < 3.0e38f) {
+        if (!(en2 == en2)) {
+            R.code = TT_RAY_NAN;
+            R.state = 3;
+        } else if (en2 >= 1.0f) {
+            const float factor = fmaxf(0.2f, 0.9f * __powf(en2, -0.1f));
+            R.hctrl = h * factor;
+            R.rejected = true;
+            if (R.hctrl < 1e-7f) {
+                R.code = TT_RAY_STEP_TOO_SMALL;
+                R.state = 3;
+            }
+        } else {
+            R.hcap = hre;  // controller state untouched: this was a geometric retry
+        }
         return;
     }
     float factor = en2 == 0.f ? 10.f : fminf(10.f, 0.9f * __powf(en2, -0.1f));

@@ -157,8 +157,10 @@ def test_f32_slab_closed_form(cuda):
     assert e["pos"] <= POS_BAR and e["ang"] <= ANG_BAR, e
 
 
-def test_f32_edge_rays(cuda):
-    """Rays outside the box, leaving through a side, starting before the box, NaN; empty call."""
+@pytest.mark.parametrize("refill", [0, 32])
+def test_f32_edge_rays(cuda, refill):
+    """Rays outside the box, leaving through a side, starting before the box, NaN; empty call.
+    refill 32: the warp takes new rays only when all its lanes are idle."""
     from turbulence_tracing_gb300 import core
 
     ne, x, _ = grf_case(n=24, L=1e-3, seed=9)
@@ -176,7 +178,7 @@ def test_f32_edge_rays(cuda):
     # discontinuity, and the outcome depends on the last bit of the start point.)
     s0[3:, 2] *= c / np.linalg.norm(s0[3:, 2])
     vol = core.build_volume(ne, x, x, x, 2, lwl=LWL)
-    out = core.trace_f32(vol, s0, R.t_end(ext), ext, rtol=1e-7, phase=True)
+    out = core.trace_f32(vol, s0, R.t_end(ext), ext, rtol=1e-7, phase=True, refill_lanes=refill)
     ref = oracle_trace(ne, x, s0)
     st = out["status"].cpu().numpy()
     assert st[4] == 3 and np.all(np.delete(st, 4) == 0)
@@ -186,6 +188,40 @@ def test_f32_edge_rays(cuda):
     assert e["pos"] <= POS_BAR and e["ang"] <= ANG_BAR and e["phase"] <= PHASE_BAR, e
     empty = core.trace_f32(vol, np.zeros((6, 0)), R.t_end(ext), ext)
     assert empty["rf"].shape == (4, 0)
+
+
+@pytest.mark.parametrize("refill", [0, 32])
+def test_f32_rays_that_miss_the_box(cuda, refill):
+    """Every ray misses the box (each lane's ray ends at its start), and a beam
+    where one ray in 40 enters: every ray finishes, the missing ones as the
+    straight line, under both lane-refill rules."""
+    from turbulence_tracing_gb300 import core
+
+    ne, x, _ = grf_case(n=24, L=1e-3, seed=9)
+    ext, c = x.max(), R.C_LIGHT
+    rng = np.random.default_rng(3)
+    n = 1000
+    s0 = np.zeros((6, n))
+    s0[0] = 3 * ext + rng.uniform(0, ext, n)
+    s0[1] = rng.uniform(-ext, ext, n)
+    s0[2] = -ext
+    s0[5] = c
+    T = R.t_end(ext)
+    vol = core.build_volume(ne, x, x, x, 2, lwl=LWL)
+    out = core.trace_f32(vol, s0, T, ext, phase=True, refill_lanes=refill)
+    assert (out["status"].cpu().numpy() == 0).all() and (out["nsteps"].cpu().numpy() == 0).all()
+    rf = out["rf"].cpu().numpy()
+    # straight along z: the same transverse position (up to the grid-unit round trip), zero angles
+    assert np.abs(rf[0] - s0[0]).max() <= 1e-12 * ext and np.abs(rf[2] - s0[1]).max() <= 1e-12 * ext
+    assert not rf[1::2].any()
+    s0[0, ::40] = rng.uniform(-0.5 * ext, 0.5 * ext, n // 40)  # these enter
+    out = core.trace_f32(vol, s0, T, ext, phase=True, refill_lanes=refill)
+    ns = out["nsteps"].cpu().numpy()
+    assert (out["status"].cpu().numpy() == 0).all() and (ns[::40] > 0).all()
+    assert (np.delete(ns, np.arange(0, n, 40)) == 0).all()
+    ref = oracle_trace(ne, x, s0[:, ::40])
+    e = errors(out["rf"].cpu().numpy()[:, ::40], ref["rf"], 2 * ext)
+    assert e["pos"] <= POS_BAR and e["ang"] <= ANG_BAR, e
 
 
 def test_f32_null_field_is_straight(cuda):

@@ -558,14 +558,15 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restric
     bool home = true;
 #pragma unroll
     for (int a = 0; a < 3; ++a) home = home && Ps[a] >= lo[a] && Ps[a] <= hi[a];
-    if (home) {
-        const float2 hab = tri2(coef[0], Ps[0], Ps[1], Ps[2]);
-        const float2 hcq = tri2(coef[1], Ps[0], Ps[1], Ps[2]);
-        H[0] = hab.x;
-        H[1] = hab.y;
-        H[2] = hcq.x;
-        q = PHASE ? hcq.y : 0.f;
-    } else {
+    // the polynomial first, on every path: the rare branch to the exact
+    // lookup then only overrides it, and the common path is one block
+    const float2 hab = tri2(coef[0], Ps[0], Ps[1], Ps[2]);
+    const float2 hcq = tri2(coef[1], Ps[0], Ps[1], Ps[2]);
+    H[0] = hab.x;
+    H[1] = hab.y;
+    H[2] = hcq.x;
+    q = PHASE ? hcq.y : 0.f;
+    if (!home) {
         const float4 r = eval_exact(nodes, G.n[0], G.n[1], G.n[2], G.st_b, G.tile_f4, G.bd, G.bd_shift,
                                     G.brick_f4, R.ci[0], R.ci[1], R.ci[2], Ps[0], Ps[1], Ps[2]);
         H[0] = r.x;

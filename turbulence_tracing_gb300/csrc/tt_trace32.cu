@@ -550,7 +550,7 @@ __device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const R
 // Right-hand side at stage position Ps (fractions in the current cell):
 // the current cell's polynomial while Ps stays within kTolE of it (never past
 // a box face), the exact lookup otherwise.
-template <bool PHASE>
+template <int PHASE>
 __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, const Ray& R,
                                            const float2 (*coef)[8], const float Ps[3], float H[3], float& q,
                                            const float* lo, const float* hi)
@@ -565,7 +565,7 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restric
     H[0] = hab.x;
     H[1] = hab.y;
     H[2] = hcq.x;
-    q = PHASE ? hcq.y : 0.f;
+    q = PHASE != 0 ? hcq.y : 0.f;
     if (!home) {
         const float4 r = eval_exact(nodes, G.n[0], G.n[1], G.n[2], G.st_b, G.tile_f4, G.bd, G.bd_shift,
                                     G.brick_f4, R.ci[0], R.ci[1], R.ci[2], Ps[0], Ps[1], Ps[2]);
@@ -576,11 +576,12 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restric
     }
 }
 
-// One attempted step.  Returns with R updated.  PHASE (the phase integrated as
-// a seventh equation) is a template parameter: a run-time flag put a branch
-// in every stage, which split the unrolled stage loop into blocks the
-// compiler schedules separately (5.7% slower with the phase on).
-template <bool PHASE>
+// One attempted step.  Returns with R updated.  PHASE is a template parameter:
+// 0 no phase, 1 the phase integrated as a seventh equation and summed in a
+// compensated FP32 pair, 2 the same summed in FP64.  As run-time flags they
+// put branches in every stage and step, which split the unrolled stage loop
+// into blocks the compiler schedules separately (5.7% and 2.1% slower).
+template <int PHASE>
 __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, Ray& R,
                                      float2 (*coef)[8])
 {
@@ -608,7 +609,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         Hs[0][0] = hab.x;
         Hs[0][1] = hab.y;
         Hs[0][2] = hcq.x;
-        q0 = PHASE ? hcq.y : 0.f;
+        q0 = PHASE != 0 ? hcq.y : 0.f;
     }
     // Predict the first face crossing of the cell from position, velocity and
     // acceleration; aim the step end at it.  Leaving through a box face within
@@ -759,7 +760,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     float dphi = 0.f;
     if (PHASE) {
         dphi = h * phb;
-        const float phv = K.phase_f64 ? (float)ph_get(R) : R.ph;
+        const float phv = (PHASE == 2) ? (float)ph_get(R) : R.ph;
         const float phn = phv + dphi;
         const float scp = K.atol_phase + K.rtol * fmaxf(fabsf(phv), fabsf(phn));
         const float x = __fdividef(h * phe, scp);
@@ -827,7 +828,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
         R.sig = t;
     }
     if (PHASE) {
-        if (K.phase_f64) ph_set(R, ph_get(R) + (double)dphi);
+        if (PHASE == 2) ph_set(R, ph_get(R) + (double)dphi);
         else neumaier(R.ph, R.phc, dphi);
     }
     if (renormalise(G, R)) R.state = 1;
@@ -852,7 +853,7 @@ __device__ __forceinline__ int instance_of(const Geo* g, int n, long long r)
 // block (src: node buffer and the block of the instance-blocked arrays).  It
 // is asked once per fetched ray; the node pointer is kept for the ray's steps
 // unless the policy has it as a constant (pol.nodes).
-template <bool PHASE, typename Policy>
+template <int PHASE, typename Policy>
 __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const double* __restrict__ s0,
                                                 long long np, const unsigned* __restrict__ perm,
                                                 unsigned long long* __restrict__ counter, double* __restrict__ sf,
@@ -911,7 +912,7 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
                     double P0[3], u0[3];
                     if (!init_ray(pol.geo(ray), src, s0, np, ray, R, P0, u0)) {
                         finish_ray<false>(pol.geo(ray), src, R, P0, u0, ray, np, sf, rf, phase, status, nsteps,
-                                          K.phase_f64 != 0);
+                                          PHASE == 2);
                         busy = false;  // picked up again on the next pass
                     }
                 } else if (nb == ne) {
@@ -934,7 +935,7 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
             step<PHASE>(pol.geo(ray), pol.nodes(nodes), K, R, coef);
             if (R.state != 0) {
                 finish_ray<true>(pol.geo(ray), pol.src(ray), R, nullptr, nullptr, ray, np, sf, rf, phase, status,
-                                 nsteps, K.phase_f64 != 0);
+                                 nsteps, PHASE == 2);
                 busy = false;
             }
         }
@@ -948,7 +949,7 @@ struct SinglePolicy {
     __device__ __forceinline__ const float4* nodes(const float4*) const { return g->nodes; }
 };
 
-template <int BLOCK, bool PHASE>
+template <int BLOCK, int PHASE>
 __global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
 trace32_kernel(const Geo G, Ctl K, const double* __restrict__ s0, long long np,
                const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
@@ -985,7 +986,7 @@ struct MixedPolicy {
     __device__ __forceinline__ const float4* nodes(const float4* kept) const { return kept; }
 };
 
-template <int BLOCK, bool PHASE>
+template <int BLOCK, int PHASE>
 __global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
 trace32_batched_kernel(const __grid_constant__ GeoTable table, Ctl K, const double* __restrict__ s0, long long np,
                        const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
@@ -1013,7 +1014,7 @@ struct UniformPolicy {
     __device__ __forceinline__ const float4* nodes(const float4* kept) const { return kept; }
 };
 
-template <int BLOCK, bool PHASE>
+template <int BLOCK, int PHASE>
 __global__ void __launch_bounds__(BLOCK, kThreadsPerSM / BLOCK)
 trace32_uniform_kernel(const __grid_constant__ GeoTable table, Ctl K, const double* __restrict__ s0,
                        long long np, const unsigned* __restrict__ perm, unsigned long long* __restrict__ counter,
@@ -1178,7 +1179,7 @@ template <typename KernelT>
 int occupancy_grid(KernelT kernel, int block, int slot)
 {
     // per-(kernel, device) cache; threads may race to fill an entry, all with the same value
-    static std::atomic<int> cache[18][64];
+    static std::atomic<int> cache[27][64];
     int dev = 0;
     cudaGetDevice(&dev);
     int b = (dev >= 0 && dev < 64) ? cache[slot][dev].load(std::memory_order_relaxed) : 0;
@@ -1240,10 +1241,12 @@ int run(const GeoTable& table, int nbins, const Ctl& K, int block, const double*
     const Ctl& Kc = K;
 #define TT_LAUNCH_ONE(KERNEL, ARGS, BS, SLOT)                                                         \
     do {                                                                                              \
-        if (Kc.with_phase)                                                                            \
-            KERNEL<BS, true><<<occupancy_grid(KERNEL<BS, true>, BS, (SLOT) + 9), BS, 0, s>>> ARGS;    \
+        if (Kc.with_phase && Kc.phase_f64)                                                            \
+            KERNEL<BS, 2><<<occupancy_grid(KERNEL<BS, 2>, BS, (SLOT) + 18), BS, 0, s>>> ARGS;         \
+        else if (Kc.with_phase)                                                                       \
+            KERNEL<BS, 1><<<occupancy_grid(KERNEL<BS, 1>, BS, (SLOT) + 9), BS, 0, s>>> ARGS;          \
         else                                                                                          \
-            KERNEL<BS, false><<<occupancy_grid(KERNEL<BS, false>, BS, SLOT), BS, 0, s>>> ARGS;        \
+            KERNEL<BS, 0><<<occupancy_grid(KERNEL<BS, 0>, BS, SLOT), BS, 0, s>>> ARGS;                \
     } while (0)
 #define TT_LAUNCH_SINGLE(BS, SLOT) \
     TT_LAUNCH_ONE(trace32_kernel, (table.g[0], Kc, s0, np, perm, counter, sf, rf, phase, status, nsteps), BS, SLOT)

@@ -213,8 +213,64 @@ __device__ __forceinline__ void poly2(float2 v000, float2 v001, float2 v010, flo
 __device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
 __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 
+// One component's polynomial, as one lane of poly2 / tri2 (the same rounding).
+__device__ __forceinline__ void poly1(float v000, float v001, float v010, float v011, float v100, float v101,
+                                      float v110, float v111, float* c)
+{
+    c[0] = v000;
+    c[1] = __fsub_rn(v100, v000);
+    c[2] = __fsub_rn(v010, v000);
+    c[3] = __fsub_rn(v001, v000);
+    const float d101 = __fsub_rn(v101, v100);
+    c[4] = __fsub_rn(__fsub_rn(v110, v100), c[2]);
+    c[5] = __fsub_rn(d101, c[3]);
+    c[6] = __fsub_rn(__fsub_rn(v011, v010), c[3]);
+    c[7] = __fsub_rn(__fsub_rn(__fsub_rn(v111, v110), d101), c[6]);
+}
+__device__ __forceinline__ float tri1(const float* c, float fa, float fb, float fc)
+{
+    const float t1 = fmaf(c[7], fc, c[4]);
+    const float t2 = fmaf(c[5], fc, c[1]);
+    const float t3 = fmaf(fb, t1, t2);
+    const float t4 = fmaf(c[6], fc, c[2]);
+    const float t5 = fmaf(c[3], fc, c[0]);
+    const float t6 = fmaf(fb, t4, t5);
+    return fmaf(fa, t3, t6);
+}
+
+// The cell's trilinear polynomials: (H_a, H_b) packed, and (H_c, q) packed
+// when the phase is integrated; without the phase H_c alone (8 registers fewer).
+template <int PHASE>
+struct CellPoly {
+    float2 ab[8];
+    float2 cq[8];
+};
+template <>
+struct CellPoly<0> {
+    float2 ab[8];
+    float c[8];
+};
+
+template <int PHASE>
+__device__ __forceinline__ void cell_eval(const CellPoly<PHASE>& cp, float fa, float fb, float fc, float H[3],
+                                          float& q)
+{
+    const float2 hab = tri2(cp.ab, fa, fb, fc);
+    H[0] = hab.x;
+    H[1] = hab.y;
+    if constexpr (PHASE == 0) {
+        H[2] = tri1(cp.c, fa, fb, fc);
+        q = 0.f;
+    } else {
+        const float2 hcq = tri2(cp.cq, fa, fb, fc);
+        H[2] = hcq.x;
+        q = hcq.y;
+    }
+}
+
+template <int PHASE>
 __device__ __forceinline__ void load_cell(const Geo& G, const float4* __restrict__ nodes, long long tbase, int ca,
-                                          int cb, int cc, float2 (*coef)[8])
+                                          int cb, int cc, CellPoly<PHASE>& cp)
 {
     const int cl = cc & (G.bd - 1);
     const int dc = (cl == G.bd - 1) ? G.brick_f4 - (G.bd - 1) : 1;
@@ -225,8 +281,11 @@ __device__ __forceinline__ void load_cell(const Geo& G, const float4* __restrict
     const float4 n010 = __ldg(p + db), n011 = __ldg(p + db + dc);
     const float4 n100 = __ldg(p + da), n101 = __ldg(p + da + dc);
     const float4 n110 = __ldg(p + da + db), n111 = __ldg(p + da + db + dc);
-    poly2(lo2(n000), lo2(n001), lo2(n010), lo2(n011), lo2(n100), lo2(n101), lo2(n110), lo2(n111), coef[0]);
-    poly2(hi2(n000), hi2(n001), hi2(n010), hi2(n011), hi2(n100), hi2(n101), hi2(n110), hi2(n111), coef[1]);
+    poly2(lo2(n000), lo2(n001), lo2(n010), lo2(n011), lo2(n100), lo2(n101), lo2(n110), lo2(n111), cp.ab);
+    if constexpr (PHASE == 0)
+        poly1(n000.z, n001.z, n010.z, n011.z, n100.z, n101.z, n110.z, n111.z, cp.c);
+    else
+        poly2(hi2(n000), hi2(n001), hi2(n010), hi2(n011), hi2(n100), hi2(n101), hi2(n110), hi2(n111), cp.cq);
 }
 
 // Square roots and reciprocals of the phase rate and the face prediction as the
@@ -552,7 +611,7 @@ __device__ __forceinline__ void finish_ray(const Geo& G, const Src& src, const R
 // a box face), the exact lookup otherwise.
 template <int PHASE>
 __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, const Ray& R,
-                                           const float2 (*coef)[8], const float Ps[3], float H[3], float& q,
+                                           const CellPoly<PHASE>& cp, const float Ps[3], float H[3], float& q,
                                            const float* lo, const float* hi)
 {
     bool home = true;
@@ -560,12 +619,7 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restric
     for (int a = 0; a < 3; ++a) home = home && Ps[a] >= lo[a] && Ps[a] <= hi[a];
     // the polynomial first, on every path: the rare branch to the exact
     // lookup then only overrides it, and the common path is one block
-    const float2 hab = tri2(coef[0], Ps[0], Ps[1], Ps[2]);
-    const float2 hcq = tri2(coef[1], Ps[0], Ps[1], Ps[2]);
-    H[0] = hab.x;
-    H[1] = hab.y;
-    H[2] = hcq.x;
-    q = PHASE != 0 ? hcq.y : 0.f;
+    cell_eval<PHASE>(cp, Ps[0], Ps[1], Ps[2], H, q);
     if (!home) {
         const float4 r = eval_exact(nodes, G.n[0], G.n[1], G.n[2], G.st_b, G.tile_f4, G.bd, G.bd_shift,
                                     G.brick_f4, R.ci[0], R.ci[1], R.ci[2], Ps[0], Ps[1], Ps[2]);
@@ -583,7 +637,7 @@ __device__ __forceinline__ void stage_eval(const Geo& G, const float4* __restric
 // into blocks the compiler schedules separately (5.7% and 2.1% slower).
 template <int PHASE>
 __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ nodes, const Ctl& K, Ray& R,
-                                     float2 (*coef)[8])
+                                     CellPoly<PHASE>& coef)
 {
     if (R.cell_dirty) {
         const int ta = R.ci[0] >> 2, tb = R.ci[1] >> 2;
@@ -604,12 +658,7 @@ __device__ __forceinline__ void step(const Geo& G, const float4* __restrict__ no
     float Hs[7][3];
     float q0;
     {  // stage 0 is at the ray's own position, always inside the current cell's range
-        const float2 hab = tri2(coef[0], R.fr[0], R.fr[1], R.fr[2]);
-        const float2 hcq = tri2(coef[1], R.fr[0], R.fr[1], R.fr[2]);
-        Hs[0][0] = hab.x;
-        Hs[0][1] = hab.y;
-        Hs[0][2] = hcq.x;
-        q0 = PHASE != 0 ? hcq.y : 0.f;
+        cell_eval<PHASE>(coef, R.fr[0], R.fr[1], R.fr[2], Hs[0], q0);
     }
     // Predict the first face crossing of the cell from position, velocity and
     // acceleration; aim the step end at it.  Leaving through a box face within
@@ -869,7 +918,7 @@ __device__ __forceinline__ void persistent_loop(Policy pol, const Ctl& K, const 
     unsigned wnext = 0, wend = 0;  // the warp's chunk of perm positions (warp-uniform)
     const float4* nodes = nullptr;
     Ray R;
-    float2 coef[2][8];
+    CellPoly<PHASE> coef;
     R.state = 1;
     for (;;) {
         const bool need = !busy && !drained;

@@ -340,8 +340,12 @@ def test_trained_surrogate_gains_and_fallback_bounds_error(cuda):
     # the shadowgrams are an order of magnitude closer to the exact trace
     assert e_n.mean() < 0.1 * e_s.mean(), (e_n.mean(), e_s.mean())
     assert np.median(ph_n) < 0.2, np.median(ph_n)
-    # and the network does not spoil the march it corrects
-    assert e_n.mean() <= 1.5 * e_m.mean(), (e_n.mean(), e_m.mean())
+    # and the network neither improves nor spoils the march it corrects: its
+    # correction keeps the mean error within 15% of the march's (measured 7%
+    # above it here; the march's residual is set by the 3-D field between the
+    # planes, which the 2-D maps do not carry, so the network's role is the
+    # error estimate behind the fallback below)
+    assert e_n.mean() <= 1.15 * e_m.mean(), (e_n.mean(), e_m.mean())
     # fallback: fields whose estimate exceeds the tolerance are traced; the accepted
     # ones stay within tolerance
     kappa = SG.calibrate(res[:24])

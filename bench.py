@@ -884,8 +884,9 @@ def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
         one()
     torch.cuda.synchronize()
     # each step ends in host arrays, so steps are timed one by one; the median
-    # step is reported (host-side copies on a shared machine vary run to run)
-    k = max(3, min(a.steps, 5))
+    # of at least 7 steps is reported (now and then a step takes ~45 ms longer
+    # in the host-side copies, which moves the median of fewer steps)
+    k = max(7, min(a.steps, 15))
     if dist:
         dist.barrier()
     times, tot = [], 0

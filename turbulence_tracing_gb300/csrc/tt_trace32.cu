@@ -1015,22 +1015,16 @@ trace32_kernel(const Geo G, Ctl K, const double* __restrict__ s0, long long np,
 struct MixedPolicy {
     const Geo* g;
     int n;
-    mutable long long last_ray;
     mutable const Geo* cur;
-    __device__ __forceinline__ const Geo& geo(long long r) const
-    {
-        if (r != last_ray) {
-            // rays reach a lane in bucket order, which is instance-major, so the
-            // lane's previous instance nearly always owns the next ray too
-            if (r < cur->ray_begin || r - cur->ray_begin >= cur->nrays) cur = g + instance_of(g, n, r);
-            last_ray = r;
-        }
-        return *cur;
-    }
+    // The lane's entry: src() is asked first for every ray the lane picks up
+    // and moves cur to that ray's instance, so geo() needs no test.
+    __device__ __forceinline__ const Geo& geo(long long) const { return *cur; }
     __device__ __forceinline__ Src src(long long r) const
     {
-        const Geo& e = geo(r);
-        return Src{e.nodes, e.ray_begin, e.nrays};
+        // rays reach a lane in bucket order, which is instance-major, so the
+        // lane's previous instance nearly always owns the next ray too
+        if (r < cur->ray_begin || r - cur->ray_begin >= cur->nrays) cur = g + instance_of(g, n, r);
+        return Src{cur->nodes, cur->ray_begin, cur->nrays};
     }
     __device__ __forceinline__ const float4* nodes(const float4* kept) const { return kept; }
 };
@@ -1042,8 +1036,8 @@ trace32_batched_kernel(const __grid_constant__ GeoTable table, Ctl K, const doub
                        double* __restrict__ sf, double* __restrict__ rf, double* __restrict__ phase,
                        int* __restrict__ status, int* __restrict__ nsteps)
 {
-    persistent_loop<PHASE>(MixedPolicy{table.g, table.n, -1, table.g}, K, s0, np, perm, counter, sf, rf, phase,
-                           status, nsteps);
+    persistent_loop<PHASE>(MixedPolicy{table.g, table.n, table.g}, K, s0, np, perm, counter, sf, rf, phase, status,
+                           nsteps);
 }
 
 // Volumes of one shape (grid, spacing, brick depth, t_end): the geometry is

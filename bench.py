@@ -879,8 +879,9 @@ def e2e_run(a, pt, rtm, ne, x, s0_host, ext_mm, det, dev, ws, dist):
 
     # warm-up: the first steps allocate the device buffers and the pinned host
     # staging buffers that later steps reuse (a solve's results alternate
-    # between two of them while the previous results are still referenced)
-    for _ in range(3):
+    # between two of them while the previous results are still referenced;
+    # after the device-timed leg this takes a few more steps to settle)
+    for _ in range(6):
         one()
     torch.cuda.synchronize()
     # each step ends in host arrays, so steps are timed one by one; the median

@@ -13,20 +13,22 @@ from tests.cases import LWL, errors, oracle_trace
 pytestmark = pytest.mark.gpu
 
 
-def _small_ensemble(**kw):
+def _small_ensemble(phase=True, **kw):
     from turbulence_tracing_gb300 import ensemble
 
     inst = ensemble.draw_instances(n_inst=7, seed=3, sizes=(24, 32, 40), rays=(200, 3000))
     inst[2]["nrays"] = 0  # an instance with no rays
-    return ensemble.Ensemble(inst, L=1e-3, det=64, phase=True, **kw).setup()
+    return ensemble.Ensemble(inst, L=1e-3, det=64, phase=phase, **kw).setup()
 
 
-@pytest.mark.parametrize("mode", ["grouped", "one_launch"])
-def test_batched_equals_single_launches(cuda, mode):
-    """grouped: one uniform-shape launch per grid size; one_launch: one mixed-shape launch."""
+@pytest.mark.parametrize("mode,phase", [("grouped", True), ("one_launch", True), ("grouped", False),
+                                        ("one_launch", False)])
+def test_batched_equals_single_launches(cuda, mode, phase):
+    """grouped: one uniform-shape launch per grid size; one_launch: one mixed-shape launch;
+    with the phase and without it (each a kernel of its own)."""
     from turbulence_tracing_gb300 import core
 
-    E = _small_ensemble(tune=False, mode=mode)
+    E = _small_ensemble(phase=phase, tune=False, mode=mode)
     torch.cuda.synchronize()
     rf_b = E.out["rf"].clone()
     ph_b = E.out["phase"].clone()
@@ -36,7 +38,8 @@ def test_batched_equals_single_launches(cuda, mode):
     for i, o in enumerate(singles):
         b, e = E.offsets[i], E.offsets[i + 1]
         assert torch.equal(core.ray_block(rf_b, 4, E.offsets, i), o["rf"])
-        assert torch.equal(ph_b[b:e], o["phase"][: e - b])
+        if phase:
+            assert torch.equal(ph_b[b:e], o["phase"][: e - b])
         assert torch.equal(ns_b[b:e], o["nsteps"][: e - b])
     assert (E.out["status"] == 0).all()
 

@@ -343,7 +343,6 @@ struct Ray {
     int code;
     bool rejected;
     bool cell_dirty;
-    bool entered;
     int ta, tb;
     long long tbase;
 };
@@ -492,7 +491,6 @@ __device__ __forceinline__ bool init_ray(const Geo& G, const Src& src, const dou
     R.hctrl = 1.0f;
     R.hcap = 3.0e38f;
     R.rejected = false;
-    R.entered = false;
     R.code = TT_RAY_OK;
     if (!finite) {
         R.code = TT_RAY_NAN;
@@ -539,7 +537,6 @@ __device__ __forceinline__ bool init_ray(const Geo& G, const Src& src, const dou
     R.sig = tin;
     R.sigc = 0.f;
     R.state = 0;
-    R.entered = true;
     R.cell_dirty = true;
     R.ta = -1;
     R.tb = -1;

@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--det", type=int, default=1024)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--block", type=int, default=0, help="FP32 tracer threads per block (0 = the library's 256)")
+    ap.add_argument("--brick-depth", type=int, default=0, help="node-volume brick depth, 4..32 (0 = the library's 8)")
+    ap.add_argument("--refill", type=int, default=0, help="FP32 tracer refill_lanes, 1..32 (0 = the library's 1)")
     ap.add_argument("--fp64-rays", type=int, default=1000000)
     ap.add_argument("--check-rays", type=int, default=20000)
     ap.add_argument("--cpu-rays", type=int, default=8000)
@@ -248,7 +250,7 @@ def run_ours(a):
     rng_mm = (-ext_mm, ext_mm)
 
     # persistent buffers so the timed steps allocate nothing
-    vol = core.build_volume(ne, x, x, x, probing_axis=2, lwl=a.lwl)
+    vol = core.build_volume(ne, x, x, x, probing_axis=2, lwl=a.lwl, brick_depth=a.brick_depth or 8)
     out = core._ray_outputs(Np, dev, want_sf=True)
     ws_bytes = _lib.lib().tt_trace_f32_workspace_bytes(__import__("ctypes").byref(vol.desc), Np)
     wsp = core.workspace(ws_bytes, dev)
@@ -266,7 +268,7 @@ def run_ours(a):
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
         core.trace_f32(vol, s0, t_end, ext, rtol=1e-7, atol=1e-5, atol_phase=1e-5, phase=True, ws=wsp, out=out,
-                       block_size=a.block)
+                       block_size=a.block, refill_lanes=a.refill)
         if record:
             e1.record()
             tr_ev.append((e0, e1))
@@ -317,7 +319,9 @@ def run_ours(a):
            "roofline": roof, "clocks": clocks,
            "detail": {"ray_steps_per_step": ray_steps_step, "rays_per_s": rays_per_s,
                       "steps_per_ray": ray_steps_step / Np, "trace_ms": trace_ms_avg,
-                      "non_ok_rays": n_bad}}
+                      "non_ok_rays": n_bad,
+                      "tracer": {"block": a.block or 256, "brick_depth": a.brick_depth or 8,
+                                 "refill_lanes": a.refill or 1}}}
 
     if not a.no_e2e:
         # right after the device-timed leg: the FP64 leg's buffers (other sizes)

@@ -65,7 +65,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--block", type=int, default=0, help="FP32 tracer threads per block (0 = the library's 256)")
     ap.add_argument("--brick-depth", type=int, default=0, help="node-volume brick depth, 4..32 (0 = the library's 8)")
-    ap.add_argument("--refill", type=int, default=0, help="FP32 tracer refill_lanes, 1..32 (0 = the library's 1)")
+    ap.add_argument("--refill", type=int, default=0, help="FP32 tracer refill_lanes, 1..32 (0 = the library's 2)")
     ap.add_argument("--fp64-rays", type=int, default=1000000)
     ap.add_argument("--check-rays", type=int, default=20000)
     ap.add_argument("--cpu-rays", type=int, default=8000)
@@ -321,7 +321,7 @@ def run_ours(a):
                       "steps_per_ray": ray_steps_step / Np, "trace_ms": trace_ms_avg,
                       "non_ok_rays": n_bad,
                       "tracer": {"block": a.block or 256, "brick_depth": a.brick_depth or 8,
-                                 "refill_lanes": a.refill or 1}}}
+                                 "refill_lanes": a.refill or 2}}}
 
     if not a.no_e2e:
         # right after the device-timed leg: the FP64 leg's buffers (other sizes)
@@ -457,8 +457,8 @@ def batched_run(a):
     launches, shadowgrams.  The ensemble's set-up times the launch forms on
     the ensemble itself (one mixed-shape launch for all instances, one
     batched launch per grid shape, or one launch per instance), each with
-    every idle lane refilled at once and with a warp's 32 lanes refilled
-    together, and keeps the fastest; the eager one-launch-per-instance form
+    the library's lane refill (a warp refills once two lanes are idle) and
+    with a warp's 32 lanes refilled together, and keeps the fastest; the eager one-launch-per-instance form
     with the tracer's defaults is timed beside it.  The same is repeated for
     small instances (2e3..8e4 rays)."""
     import torch
@@ -580,7 +580,7 @@ def surrogate_run(a):
     # detector set-up: each field's drift for 20% straight-line contrast
     Ds = [float(W.drift(W.maps(f))) for f in fields]
     pipe = SG.Pipeline(W, net, kappa, batch=a.sur_batch)
-    bts = {rl: SG.BatchedTracer(W, batch=a.sur_batch, refill_lanes=rl) for rl in (1, 32)}
+    bts = {rl: SG.BatchedTracer(W, batch=a.sur_batch, refill_lanes=rl) for rl in (2, 32)}
     pipe.run(fields[:a.sur_batch], Ds[:a.sur_batch])
     pipe.run_tracer(fields[:2], Ds[:2])
     for bt in bts.values():

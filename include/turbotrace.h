@@ -153,7 +153,7 @@ typedef struct tt_trace_opts {
     int32_t phase_f64;  /* FP32 tracer with phase: accumulate the phase sum in FP64 (one double add
                            per accepted step) instead of a Neumaier-compensated FP32 pair */
     int32_t refill_lanes; /* FP32 tracer: a warp takes new rays only once at least this many of its
-                           32 lanes are idle, 1..32 (0 = 1).  1 refills every idle lane at once;
+                           32 lanes are idle, 1..32 (0 = 2).  1 refills every idle lane at once;
                            32 traces each warp's 32 neighbouring rays to the end together, which
                            keeps the lanes' node reads coherent.  Results do not depend on it. */
 } tt_trace_opts;

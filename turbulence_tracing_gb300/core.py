@@ -309,7 +309,7 @@ def trace_f32(vol, s0, t_end, extent, rtol=1e-7, atol=1e-5, atol_phase=1e-5, pha
               want_sf=True, ws=None, out=None, block_size=0, ray_chunk=0, phase_f64=False, refill_lanes=0):
     """Persistent FP32 tracer over a Volume32.  s0: (6, Np) float64.
     phase_f64: accumulate the phase in FP64 rather than a compensated FP32 pair.
-    refill_lanes: a warp takes new rays once this many lanes are idle (0 = 1;
+    refill_lanes: a warp takes new rays once this many lanes are idle (0 = 2;
     32 keeps a warp on 32 neighbouring rays to the end; results are the same)."""
     dev = require_cuda()
     L = _lib.lib()

@@ -33,7 +33,7 @@ import torch
 from . import _lib, autotune, core, turboGen
 
 C_LIGHT = 299792458.0
-REFILLS = (1, 32)  # lane refill thresholds the set-up times (tt_trace_opts.refill_lanes)
+REFILLS = (2, 32)  # lane refill thresholds the set-up times (tt_trace_opts.refill_lanes; 2 is the library's default)
 
 
 def draw_instances(n_inst=64, seed=0, sizes=(128, 192, 256, 384), exponents=(-5.0 / 3.0, -3.0, -11.0 / 3.0),
@@ -66,7 +66,7 @@ def gaussian_beam_into(dst, nrays, sigma, divergence, extent, rng):
 
 class Ensemble:
     def __init__(self, instances, L=2e-3, sigma_frac=0.25, divergence=0.05e-3, lwl=1064e-9, det=512,
-                 phase=False, rtol=1e-7, tune=True, tune_rays=200000, beam_seed=1, mode="grouped", refill_lanes=1):
+                 phase=False, rtol=1e-7, tune=True, tune_rays=200000, beam_seed=1, mode="grouped", refill_lanes=2):
         order = sorted(range(len(instances)), key=lambda i: instances[i]["n"])
         self.order = order  # instance k here is instances[order[k]]
         self.inst = [instances[i] for i in order]
@@ -141,8 +141,8 @@ class Ensemble:
         self.step()  # allocates outputs and workspace once
         torch.cuda.synchronize()
         if self.tune:
-            # launch mode and lane refill (every idle lane at once, or a warp's
-            # 32 lanes together), then the block size, timed on the ensemble itself
+            # launch mode and lane refill (the library's default, or a warp's 32
+            # lanes together), then the block size, timed on the ensemble itself
             self.mode_ms = {}
             for m in ("grouped", "per_instance", "one_launch"):
                 for rl in REFILLS:

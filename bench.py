@@ -43,7 +43,7 @@ ALG_BYTES_PHASE = 768  # 6 stages x 8 corners x 4 components x 4 B per ray-step 
 # DRAM bytes.  The bench line scales them by accepted ray-steps for other
 # workloads and says so.
 TRACE32_CAPTURE = {"workload": "grf512_1e+07rays_phase_3det1024", "ray_steps": 4225457556,
-                   "warp_inst": 143187387444, "dram_read_bytes": 20879546624, "dram_write_bytes": 5859549696}
+                   "warp_inst": 143832795789, "dram_read_bytes": 20968995072, "dram_write_bytes": 6026149376}
 
 
 def parse():

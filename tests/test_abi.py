@@ -100,6 +100,34 @@ def test_trace_f32_options_checked_before_any_launch():
                           None, 0, None) == 1
 
 
+def test_trace_f32_batched_arguments_checked_before_any_launch():
+    """Instance count (1..TT_MAX_INSTANCES) and the ray offsets are checked
+    before the batched tracer touches the device."""
+    from turbulence_tracing_gb300 import _lib, core
+
+    L = _lib.lib()
+    x = np.linspace(-1e-3, 1e-3, 20)
+    v = core.volume_plan((20, 20, 20), x, x, x, 2, 1064e-9)
+    v.nodes = ctypes.c_void_p(256)  # never dereferenced: no ray is traced
+    n = _lib.MAX_INSTANCES + 1
+    descs = (_lib.TTVolume * n)(*([v] * n))
+    o = core._opts(1e-7, 1e-5, 1e-5, None, False)
+    dp = ctypes.POINTER(ctypes.c_double)
+
+    def call(ninst, offs):
+        offs = np.ascontiguousarray(offs, dtype=np.int64)
+        te = np.full(max(ninst, 1), 1e-11)
+        return L.tt_trace_f32_batched(descs, ninst, offs.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                      te.ctypes.data_as(dp), te.ctypes.data_as(dp), None, ctypes.byref(o), None,
+                                      None, None, None, None, None, 0, None)
+
+    assert call(_lib.MAX_INSTANCES, np.zeros(_lib.MAX_INSTANCES + 1)) == 0  # all empty: nothing to trace
+    assert call(n, np.zeros(n + 1)) == 1
+    assert call(0, np.zeros(1)) == 1
+    assert call(2, [1, 2, 3]) == 1       # offsets must start at 0
+    assert call(2, [0, 5, 3]) == 1       # and not decrease
+
+
 def test_no_gpu_means_loud_failure():
     import torch
 

@@ -44,6 +44,33 @@ def test_batched_equals_single_launches(cuda, mode, phase):
     assert (E.out["status"] == 0).all()
 
 
+def test_batched_at_the_instance_limit(cuda):
+    """TT_MAX_INSTANCES volumes of mixed shapes in one launch (the whole table
+    a kernel parameter): every instance equals its own single launch."""
+    from turbulence_tracing_gb300 import _lib, core
+
+    n = _lib.MAX_INSTANCES
+    rng = np.random.default_rng(7)
+    vols, s0s, xs = [], [], []
+    for i in range(n):
+        m = int(rng.choice((10, 12, 14)))
+        ne, x = R.workload_density(m, 1e-3, -11 / 3, 0.2, 1e24, i)
+        vols.append(core.build_volume(ne, x, x, x, 2, lwl=LWL))
+        s0s.append(R.gaussian_beam(int(rng.integers(1, 80)), 0.25e-3, 1e-4, x.max(), rng))
+        xs.append(x)
+    offs = np.concatenate([[0], np.cumsum([s.shape[1] for s in s0s])])
+    flat = np.concatenate([s.reshape(-1) for s in s0s])
+    t_ends = [R.t_end(x.max()) for x in xs]
+    ext = [x.max() for x in xs]
+    for rl in (0, 32):
+        o = core.trace_f32_batched(vols, flat, offs, t_ends, ext, phase=True, refill_lanes=rl)
+        for i in (0, 1, n // 2, n - 1):
+            single = core.trace_f32(vols[i], s0s[i], t_ends[i], ext[i], phase=True)
+            assert torch.equal(core.ray_block(o["rf"], 4, offs, i), single["rf"]), (rl, i)
+            assert torch.equal(o["nsteps"][offs[i]:offs[i + 1]], single["nsteps"]), (rl, i)
+        assert (o["status"] == 0).all()
+
+
 def test_batched_instance_against_oracle(cuda):
     from turbulence_tracing_gb300 import core
 
